@@ -1,0 +1,50 @@
+#ifndef DMG_INTERNAL_H
+#define DMG_INTERNAL_H
+/* Internal helpers shared by the host-side C sources. */
+#include <stdint.h>
+#include "reshape.h"
+#include "dmg_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Record an error with a code; returns the code. */
+int dmg_error(int code, const char *fmt, ...);
+
+/* Sentinel added to an address table entry for a coordinate that a side does
+ * not hold.  Eight of them still sum to a negative int64, and no real address
+ * comes near 2^58 elements. */
+#define DMG_ABSENT (-(((int64_t)1) << 58))
+
+/* Position of virtual rank r along axis a: (r / rank_stride) % proc_size
+ * (reference reshape.c:72). */
+static inline int dmg_axis_pos(AxisDecomp a, int r) {
+  return (r / a->rank_stride) % a->decomp->proc_size;
+}
+
+/* Is the virtual comm valid. */
+int dmg_comm_ok(MPI_Comm comm);
+
+/* Per-virtual-rank memory stride of axis a. */
+static inline long long dmg_axis_stride(AxisDecomp a, int r) {
+  return a->rank_memory_stride ? a->rank_memory_stride[r] : (long long)a->memory_stride;
+}
+
+/* Does virtual rank r hold data in d (every axis has local points at r's position). */
+int dmg_rank_holds(Decomp d, int r);
+
+/* Order of dimensions, fastest first, computed from the src strides seen by
+ * rank r (reference reshape.c:330-350). */
+void dmg_sort_order(int ndim, int *order, Decomp src, int r);
+
+/* Device-side helpers implemented in the CUDA sources. */
+int dmg_dev_alloc(void **ptr, size_t bytes);
+void dmg_dev_free(void *ptr);
+int dmg_dev_upload(void *dst, const void *src, size_t bytes);
+void *dmg_current_stream(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
