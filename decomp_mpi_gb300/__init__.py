@@ -1,0 +1,8 @@
+"""decomp_mpi_gb300: single-GPU GB300 (sm_103a) implementation of Decomp_MPI's
+decomposition-driven reshape and split 3D FFT.
+
+The product is the C-ABI shared library ``libdecomp_gb300.so`` (headers in
+``include/``); this package builds it and mirrors its interface in Python.
+"""
+from .api import Comm, Decomp, DecompError, ReshapePlan, decomp_from_spec  # noqa: F401
+from .build import LIB_PATH, build  # noqa: F401

@@ -1,0 +1,425 @@
+"""Python mirror of the reference's reshape / split-FFT interface.
+
+Thin objects over the C-ABI library (``libdecomp_gb300.so``).  The names
+follow the reference (reshape.h, split_fft.h): a :class:`Comm` is a virtual
+communicator over ``P`` virtual ranks, a :class:`Decomp` a decomposition of
+a global array over them, a :class:`ReshapePlan` the move between two of
+them.  Device buffers are passed as raw pointers (``tensor.data_ptr()``) to
+virtual-grid arrays: rank ``r``'s local buffer starts at element
+``r * pitch``.
+"""
+from __future__ import annotations
+
+import ctypes
+import re
+
+from ._lib import DecompError, check, last_error, load
+
+__all__ = [
+    "Comm", "Decomp", "ReshapePlan", "SplitPlan", "decomp_from_spec", "processor_grid", "DecompError",
+    "FFTW_FORWARD", "FFTW_BACKWARD", "C128", "C64",
+]
+
+FFTW_FORWARD = -1
+FFTW_BACKWARD = 1
+C128 = 0
+C64 = 1
+
+
+class _DecompStruct(ctypes.Structure):
+    _fields_ = [("ndim", ctypes.c_int), ("comm", ctypes.c_void_p), ("proc_used", ctypes.c_int),
+                ("dims", ctypes.c_void_p)]
+
+
+class Comm:
+    """Virtual communicator of ``nranks`` virtual ranks (replaces MPI_Comm)."""
+
+    def __init__(self, nranks: int):
+        self.lib = load()
+        self.h = self.lib.dmg_comm_create(int(nranks))
+        if not self.h:
+            raise DecompError("dmg_comm_create(%d): %s" % (nranks, last_error()))
+        self.size = int(nranks)
+        self._children = []
+
+    def set_view_rank(self, rank: int):
+        check(self.lib.dmg_comm_set_rank(self.h, int(rank)), "dmg_comm_set_rank")
+
+    def __del__(self):
+        # descriptors made on the communicator hold a pointer to it; free it last
+        if getattr(self, "h", None) and not self._children:
+            self.lib.dmg_comm_free(self.h)
+            self.h = None
+
+
+# ------------------------------------------------------------------ DimDecomp builders
+
+def _dim(kind, *args):
+    lib = load()
+    f = {
+        "block": lib.makeBlockDecomp,
+        "blockf": lib.makeBlockDecompWithFactor,
+        "local": lib.makeLocalDecomp,
+        "single": lib.makeSingleDecomp,
+    }[kind]
+    h = f(*[int(a) for a in args])
+    if not h:
+        raise DecompError("make %s%r failed" % (kind, args))
+    return h
+
+
+def _wrap(kind, nested, *args):
+    """Decorators clone `nested`; the caller's copy is freed here."""
+    lib = load()
+    if kind == "rotate":
+        h = lib.makeRotatedDecomp(int(args[0]), nested)
+    elif kind == "interleave":
+        h = lib.makeInterleaveDecomp(nested, int(args[0]))
+    elif kind == "frev":
+        h = lib.makeFactorReverseDecomp(int(args[0]), int(args[1]), nested)
+    else:
+        raise ValueError(kind)
+    lib.freeDimDecomp(nested)
+    if not h:
+        raise DecompError("make %s%r failed" % (kind, args))
+    return h
+
+
+_TOKEN = re.compile(r"\s*([A-Za-z_]+|-?\d+|[(),|@:])")
+
+
+def _tokens(s):
+    pos, out = 0, []
+    while pos < len(s):
+        m = _TOKEN.match(s, pos)
+        if not m:
+            if s[pos:].strip() == "":
+                break
+            raise ValueError("bad decomposition spec near %r" % s[pos:])
+        out.append(m.group(1))
+        pos = m.end()
+    return out
+
+
+class _SpecParser:
+    """Parser of decomposition spec strings (see decomp_from_spec)."""
+
+    def __init__(self, text):
+        self.t = _tokens(text)
+        self.i = 0
+
+    def peek(self):
+        return self.t[self.i] if self.i < len(self.t) else None
+
+    def take(self, want=None):
+        tok = self.peek()
+        if tok is None or (want is not None and tok != want):
+            raise ValueError("spec: expected %r got %r" % (want, tok))
+        self.i += 1
+        return tok
+
+    def num(self):
+        return int(self.take())
+
+    def dim(self):
+        kind = self.take()
+        self.take("(")
+        if kind in ("block", "local", "single", "blockf"):
+            n = {"block": 2, "local": 1, "single": 3, "blockf": 3}[kind]
+            args = [self.num()]
+            for _ in range(n - 1):
+                self.take(",")
+                args.append(self.num())
+            self.take(")")
+            return _dim(kind, *args)
+        if kind == "rotate":
+            r = self.num()
+            self.take(",")
+            nested = self.dim()
+            self.take(")")
+            return _wrap("rotate", nested, r)
+        if kind == "interleave":
+            nested = self.dim()
+            self.take(",")
+            b = self.num()
+            self.take(")")
+            return _wrap("interleave", nested, b)
+        if kind == "frev":
+            a = self.num()
+            self.take(",")
+            b = self.num()
+            self.take(",")
+            nested = self.dim()
+            self.take(")")
+            return _wrap("frev", nested, a, b)
+        raise ValueError("spec: unknown decomposition %r" % kind)
+
+
+class Decomp:
+    """An N-D decomposition (owns its C handle)."""
+
+    def __init__(self, comm: Comm, handle):
+        if not handle:
+            raise DecompError("decomposition failed: %s" % last_error())
+        self.comm = comm
+        self.h = handle
+        self.lib = load()
+        comm._children.append(self)
+
+    @property
+    def _s(self):
+        return _DecompStruct.from_address(self.h)
+
+    @property
+    def ndim(self) -> int:
+        return self._s.ndim
+
+    @property
+    def proc_used(self) -> int:
+        return self._s.proc_used
+
+    def extent(self) -> int:
+        """Largest per-rank extent: the default pitch of a virtual-grid array."""
+        return int(self.lib.extent64(self.h))
+
+    def rank_extent(self, r: int) -> int:
+        return int(self.lib.rankExtent64(self.h, int(r)))
+
+    def owner(self, pos) -> int:
+        arr = (ctypes.c_int * len(pos))(*pos)
+        return self.lib.ownerRank(self.h, arr)
+
+    def global_offset(self, pos, pitch=None) -> int:
+        arr = (ctypes.c_int * len(pos))(*pos)
+        return int(self.lib.globalOffset64(self.h, arr, int(self.extent() if pitch is None else pitch)))
+
+    def free(self):
+        if self.h:
+            self.lib.freeDecomp(self.h)
+            self.h = None
+            if self in self.comm._children:
+                self.comm._children.remove(self)
+
+
+def decomp_from_spec(comm: Comm, spec: str) -> Decomp:
+    """Build a Decomp from a spec string.
+
+    ``packed:d0|d1|...`` (makePackedDecomp) or
+    ``axes:d0@stride,rank_stride|...`` (makeAxisDecomp + makeDecomp), each
+    ``d`` one of ``block(len,procs)``, ``blockf(len,factor,procs)``,
+    ``local(len)``, ``single(len,rank,procs)``, ``rotate(r,d)``,
+    ``interleave(d,B)``, ``frev(A,B,d)``.
+    """
+    lib = load()
+    spec = spec.strip()
+    if spec.startswith("packed:"):
+        p = _SpecParser(spec[len("packed:"):])
+        dims = [p.dim()]
+        while p.peek() == "|":
+            p.take("|")
+            dims.append(p.dim())
+        if p.peek() is not None:
+            raise ValueError("trailing spec text")
+        arr = (ctypes.c_void_p * len(dims))(*dims)
+        return Decomp(comm, lib.makePackedDecomp(comm.h, len(dims), arr))
+    if spec.startswith("axes:"):
+        p = _SpecParser(spec[len("axes:"):])
+        axes = []
+        while True:
+            d = p.dim()
+            p.take("@")
+            stride = p.num()
+            p.take(",")
+            rs = p.num()
+            a = lib.makeAxisDecomp(comm.h, d, stride, rs)
+            if not a:
+                raise DecompError("makeAxisDecomp: %s" % last_error())
+            axes.append(a)
+            if p.peek() != "|":
+                break
+            p.take("|")
+        arr = (ctypes.c_void_p * len(axes))(*axes)
+        return Decomp(comm, lib.makeDecomp(len(axes), arr))
+    raise ValueError("spec must start with packed: or axes:")
+
+
+class ReshapePlan:
+    """makeReshapePlan / runReshapePlan on the virtual grid."""
+
+    def __init__(self, comm: Comm, elem_bytes: int, src: Decomp, dest: Decomp):
+        self.lib = load()
+        self.comm, self.src, self.dest = comm, src, dest
+        self.h = self.lib.makeReshapePlan(comm.h, int(elem_bytes), src.h, dest.h)
+        if not self.h:
+            raise DecompError("makeReshapePlan: %s" % last_error())
+        self.elem_bytes = int(elem_bytes)
+
+    def set_pitch(self, src_pitch=0, dest_pitch=0):
+        check(self.lib.dmg_reshape_set_pitch(self.h, int(src_pitch), int(dest_pitch)), "dmg_reshape_set_pitch")
+
+    @property
+    def src_pitch(self) -> int:
+        return int(self.lib.dmg_reshape_pitch(self.h, 0))
+
+    @property
+    def dest_pitch(self) -> int:
+        return int(self.lib.dmg_reshape_pitch(self.h, 1))
+
+    @property
+    def bytes_moved(self) -> int:
+        return int(self.lib.dmg_reshape_bytes(self.h))
+
+    @property
+    def elements(self) -> int:
+        return int(self.lib.dmg_reshape_elements(self.h))
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.dmg_reshape_launches(self.h))
+
+    def describe(self) -> str:
+        return self.lib.dmg_reshape_describe(self.h).decode()
+
+    def run(self, src_ptr: int, dest_ptr: int, stream=None):
+        """Enqueue the reshape on `stream` (a CUDA stream handle, int; None = default stream)."""
+        check(self.lib.dmg_reshape_run(self.h, ctypes.c_void_p(src_ptr), ctypes.c_void_p(dest_ptr),
+                                       ctypes.c_void_p(stream or 0)), "runReshapePlan")
+
+    def check_bounds(self, type_size: int, src_len: int, dest_len: int) -> int:
+        return self.lib.checkReshapePlanBounds(self.h, int(type_size), int(src_len), int(dest_len))
+
+    def free(self):
+        if self.h:
+            self.lib.freeReshapePlan(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def _int_array(vals):
+    return (ctypes.c_int * len(vals))(*[int(v) for v in vals])
+
+
+def processor_grid(comm: Comm, tasks):
+    """makeProcessorGrid: the reference's grid search over the communicator's ranks."""
+    lib = load()
+    ptr = lib.makeProcessorGrid(comm.h, len(tasks), _int_array(tasks))
+    if not ptr:
+        raise DecompError("makeProcessorGrid: %s" % last_error())
+    out = [ptr[i] for i in range(len(tasks))]
+    ctypes.CDLL(None).free(ctypes.cast(ptr, ctypes.c_void_p))
+    return out
+
+
+class _SplitStruct(ctypes.Structure):
+    _fields_ = [("comm", ctypes.c_void_p), ("A_factors", ctypes.POINTER(ctypes.c_int)), ("A", ctypes.c_void_p),
+                ("B", ctypes.c_void_p), ("B_flipped", ctypes.c_void_p), ("src", ctypes.c_void_p),
+                ("work", ctypes.c_void_p), ("extent", ctypes.c_int), ("plan_a", ctypes.c_void_p),
+                ("plan_b", ctypes.c_void_p), ("plan_a_back", ctypes.c_void_p), ("plan_b_back", ctypes.c_void_p),
+                ("start_to_A", ctypes.c_void_p), ("A_to_start", ctypes.c_void_p), ("A_to_B", ctypes.c_void_p),
+                ("B_to_A", ctypes.c_void_p), ("twiddle", ctypes.c_void_p),
+                ("times", ctypes.POINTER(ctypes.c_double)), ("impl", ctypes.c_void_p)]
+
+
+class _BorrowedDecomp(Decomp):
+    """A Decomp owned by a plan (not freed from Python)."""
+
+    def __init__(self, comm, handle):
+        self.comm, self.h, self.lib = comm, handle, load()
+
+    def free(self):
+        pass
+
+
+class SplitPlan:
+    """Split 3D FFT plan (makeSplitPlan / makeParallelPlan / autotuneParallelPlan).
+
+    ``dat`` and ``work`` are device pointers; ``length`` is the per-rank
+    workspace length in elements.  ``dtype`` is C128 (FP64) or C64 (FP32).
+    """
+
+    def __init__(self, start: Decomp, dat_ptr: int, length: int, work_ptr: int, slab: int = 0, B=None,
+                 dtype: int = C128, autotune: bool = False):
+        self.lib = load()
+        self.start = start
+        if autotune:
+            if dtype != C128:
+                raise ValueError("autotuneParallelPlan is complex128")
+            h = self.lib.autotuneParallelPlan(start.h, ctypes.c_void_p(dat_ptr), int(length), ctypes.c_void_p(work_ptr))
+        elif B is not None:
+            h = self.lib.dmg_makeParallelPlanTyped(start.h, _int_array(B), ctypes.c_void_p(dat_ptr), int(length),
+                                                   ctypes.c_void_p(work_ptr), int(dtype))
+        else:
+            h = self.lib.dmg_makeSplitPlanTyped(int(slab), start.h, ctypes.c_void_p(dat_ptr), int(length),
+                                                ctypes.c_void_p(work_ptr), int(dtype))
+        if not h:
+            raise DecompError("split plan: %s" % last_error())
+        self.h = h
+        self.length = int(length)
+        self.dtype = dtype
+
+    @property
+    def _s(self):
+        return _SplitStruct.from_address(self.h)
+
+    @property
+    def ndim(self):
+        return self.start.ndim
+
+    @property
+    def A_factors(self):
+        s = self._s
+        return [s.A_factors[i] for i in range(self.ndim)]
+
+    @property
+    def extent(self):
+        return self._s.extent
+
+    def decomp_A(self):
+        return _BorrowedDecomp(self.start.comm, self._s.A)
+
+    def decomp_B(self):
+        return _BorrowedDecomp(self.start.comm, self._s.B) if self._s.B else None
+
+    def transformed(self):
+        """getTransformed(): the reference's descriptor (right only when A_i == B_i)."""
+        return _BorrowedDecomp(self.start.comm, self.lib.getTransformed(self.h))
+
+    def transformed_exact(self):
+        """getTransformedExact(): a new Decomp owned by the caller."""
+        return Decomp(self.start.comm, self.lib.getTransformedExact(self.h))
+
+    def set_buffers(self, dat_ptr, work_ptr):
+        check(self.lib.dmg_split_set_buffers(self.h, ctypes.c_void_p(dat_ptr), ctypes.c_void_p(work_ptr)),
+              "dmg_split_set_buffers")
+
+    def set_dat_pitch(self, pitch):
+        check(self.lib.dmg_split_set_dat_pitch(self.h, int(pitch)), "dmg_split_set_dat_pitch")
+
+    def run(self, direction=FFTW_FORWARD, stream=None):
+        check(self.lib.dmg_split_run(self.h, int(direction), ctypes.c_void_p(stream or 0)), "runSplitPlan")
+
+    def launches(self, direction=FFTW_FORWARD):
+        return self.lib.dmg_split_launches(self.h, int(direction))
+
+    @property
+    def flops(self):
+        return float(self.lib.dmg_split_flops(self.h))
+
+    def describe(self):
+        return self.lib.dmg_split_describe(self.h).decode()
+
+    def free(self):
+        if getattr(self, "h", None):
+            self.lib.freeSplitPlan(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass

@@ -38,6 +38,16 @@ int dmg_rank_holds(Decomp d, int r);
  * rank r (reference reshape.c:330-350). */
 void dmg_sort_order(int ndim, int *order, Decomp src, int r);
 
+/* Proper processor grid: rank = sum rank_stride_i * pos_i inverts the
+ * positions for every data-holding rank and no rank holds a copy of
+ * another's data.  DMG_OK or an error code (recorded). */
+int dmg_check_proper_grid(Decomp D, const char *side);
+
+/* Split-plan autotuner: times candidate factorisations on the GPU. */
+struct split_fft_plan;
+struct split_fft_plan *dmg_autotune_split(Decomp start, void *dat, long long length, void *workspace, int dtype,
+                                          int full_grid_search);
+
 /* Device-side helpers implemented in the CUDA sources. */
 int dmg_dev_alloc(void **ptr, size_t bytes);
 void dmg_dev_free(void *ptr);

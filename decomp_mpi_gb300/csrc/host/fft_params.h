@@ -1,0 +1,63 @@
+#ifndef DMG_FFT_PARAMS_H
+#define DMG_FFT_PARAMS_H
+/*
+ * Launch parameters of one FFT pass, shared by the C planner and the CUDA
+ * source.
+ *
+ * The global coordinate of dimension d is split as x_d = y_d + A_d * z_d
+ * (y_d < A_d, z_d < B_d).  Sub-axis s (0..5) is y of dim s/2 when s is even
+ * and z of dim s/2 when s is odd.  A pass transforms every line along one
+ * sub-axis t (length n) and moves the data from an input layout to an
+ * output layout, each given by per-dimension address tables over x_d.
+ *
+ * A block holds a tile of n x M1 x M2 values: the transform sub-axis t and
+ * two vector sub-axes v1, v2 (lines next to each other in memory), and
+ * loads/stores them in the orders that make the accesses contiguous.
+ */
+#include <stdint.h>
+
+#define DMG_FFT_MAXDIM 3
+#define DMG_FFT_MAXFAC 16
+
+struct dmg_fft_layout {
+  const int64_t *tab[DMG_FFT_MAXDIM]; /* separable: address part per x_d; ranked: type offset */
+  const int32_t *rk[DMG_FFT_MAXDIM];  /* ranked: rank part per x_d */
+  const int64_t *rstride;             /* ranked: [ndim][nranks] strides */
+  int64_t pitch;                      /* ranked: elements per virtual rank */
+  int64_t base;                       /* element offset added to every address */
+  int32_t nranks;
+  int32_t ranked;
+};
+
+struct dmg_fft_pass {
+  int32_t ndim;
+  int32_t A[DMG_FFT_MAXDIM], B[DMG_FFT_MAXDIM], L[DMG_FFT_MAXDIM];
+  int32_t t, v1, v2;           /* sub-axes (v1/v2 = -1 when absent) */
+  int32_t n, nv1, nv2;         /* their lengths */
+  int32_t M1, M2;              /* tile extents along v1, v2 */
+  int32_t nt1, nt2;            /* tiles along v1, v2 */
+  int32_t nbatch;
+  int32_t bsub[6], blen[6];    /* batch sub-axes and lengths */
+  int64_t ntiles;
+  int32_t load_order[3];       /* tile axes (0 = t, 1 = v1, 2 = v2), fastest first */
+  int32_t store_order[3];
+  int32_t nfac;
+  int32_t fac[DMG_FFT_MAXFAC]; /* radices, first stage first */
+  const void *roots;           /* n roots exp(-2 pi i k / n), double2 or float2 */
+  int32_t sign;                /* -1 forward, +1 inverse */
+  int32_t twiddle;             /* 0 none, 1 multiply after the transform, 2 multiply by the conjugate before */
+  const void *tw[DMG_FFT_MAXDIM]; /* per dim: L_d roots exp(-2 pi i m / L_d) */
+  struct dmg_fft_layout in, out;
+};
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+/* dtype 0: complex128 (FP64), 1: complex64 (FP32). */
+int dmg_fft_pass_launch(const struct dmg_fft_pass *p, int dtype, const void *src, void *dst, void *stream);
+/* Shared memory bytes a pass needs. */
+size_t dmg_fft_pass_smem(const struct dmg_fft_pass *p, int dtype);
+#ifdef __cplusplus
+}
+#endif
+#endif

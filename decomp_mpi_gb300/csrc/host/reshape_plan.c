@@ -70,7 +70,7 @@ static void side_free(side_raw *s) {
 /* Checks that rank = sum rank_stride_i * pos_i inverts pos_i = (rank /
  * rank_stride_i) % proc_size_i for every data-holding position tuple, and
  * that no other rank below proc_used holds a copy of some tuple's data. */
-static int check_proper_grid(Decomp D, const char *side) {
+int dmg_check_proper_grid(Decomp D, const char *side) {
   int nd = D->ndim;
   /* sufficient mixed-radix condition */
   int ok = 1;
@@ -177,7 +177,7 @@ static int side_build(side_raw *s, Decomp D, const char *side) {
     for (int i = 0; i < nd; ++i)
       for (int r = 0; r < P; ++r) s->rstride[(size_t)i * P + r] = dmg_axis_stride(D->dims[i], r);
   }
-  return check_proper_grid(D, side);
+  return dmg_check_proper_grid(D, side);
 }
 
 /* Address (elements) of coordinate g on a side, -1 when the side does not hold it. */

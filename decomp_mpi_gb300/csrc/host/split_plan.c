@@ -1,0 +1,874 @@
+/*
+ * Split (two-stage) 3D FFT plans on the virtual grid.
+ *
+ * Planning follows the reference (split_fft.c:36-77, 249-614, 747-788): the
+ * same factor choice, processor grids, A (interleaved) and B (blocked)
+ * decompositions, workspace check and output descriptor, so that the result
+ * lands in the same slots of the workspace.  Execution is different: instead
+ * of reshape -> FFTW -> twiddle -> reshape -> FFTW, every dimension's stage-1
+ * and stage-2 transform is one GPU pass that gathers its lines from the
+ * previous layout through address tables, so the reshapes and the twiddle are
+ * fused into the transforms.  A forward run is
+ *   stage 1: one pass per dimension with B_d > 1 (last dimension first),
+ *            the first reading `dat` in the start layout, all writing the A
+ *            layout, the last multiplying by the twiddle;
+ *   stage 2: one pass per dimension with A_d > 1, the first reading the A
+ *            layout (the A->B move), all writing the B layout;
+ * alternating between the two halves of each rank's workspace so that the
+ * last pass writes workspace[r*length + 0 ..).  The inverse runs the passes
+ * in reverse with the conjugate twiddle and ends in `dat`.
+ */
+#include <limits.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include "dmg_internal.h"
+#include "fft_params.h"
+#include "k1_params.h"
+#include "split_fft.h"
+#include "block_decomp.h"
+#include "interleave_decomp.h"
+#include "factor_reverse_decomp.h"
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+#define MAXPASS (2 * DMG_FFT_MAXDIM)
+#define TILE_TARGET 2048
+
+enum { LAY_START = 0, LAY_A = 1, LAY_B = 2 };
+enum { BUF_DAT = 0, BUF_WORK = 1 };
+
+typedef struct {
+  int ranked;
+  int nranks;
+  int64_t pitch;
+  int32_t *rk[DMG_FFT_MAXDIM];
+  int64_t *tab[DMG_FFT_MAXDIM];
+  int64_t *rstride; /* [ndim][nranks] */
+  /* device copies */
+  const int64_t *d_tab[DMG_FFT_MAXDIM];
+  const int32_t *d_rk[DMG_FFT_MAXDIM];
+  const int64_t *d_rstride;
+} fft_layout;
+
+typedef struct {
+  struct dmg_fft_pass p;
+  int in_lay, out_lay;      /* LAY_* */
+  int in_buf, out_buf;      /* BUF_* */
+  int64_t in_base, out_base;
+} pass_rec;
+
+struct dmg_split_impl {
+  int dtype; /* DMG_C128 or DMG_C64 */
+  int esize; /* bytes per element */
+  int ndim;
+  int A[DMG_FFT_MAXDIM], B[DMG_FFT_MAXDIM], L[DMG_FFT_MAXDIM];
+  int grid_a[DMG_FFT_MAXDIM], grid_b[DMG_FFT_MAXDIM];
+  int use_first, use_second;
+  long long length;    /* per-rank workspace length */
+  long long ext;       /* largest extent of A and B */
+  long long dat_pitch; /* per-rank pitch of dat */
+  Decomp start;        /* borrowed */
+  fft_layout lay[3];
+  pass_rec fwd[MAXPASS], inv[MAXPASS];
+  int nfwd, ninv;
+  void *dev; /* one device allocation for every table */
+  int dev_valid;
+  void *dat, *work;
+  int timing;
+  void *events;
+  char desc[768];
+};
+
+/* timing helpers live in the CUDA runtime source */
+void *dmg_split_create_events(int count);
+void dmg_split_destroy_events(void *ev);
+int dmg_split_record_event(void *ev, int idx, void *stream);
+int dmg_split_event_elapsed(void *ev, int a, int b, float *ms);
+
+/* ---------------------------------------------------------------- decomposition builders */
+
+Decomp makeInterleavedDecomp(int ndim, MPI_Comm comm, int A[], int B[], int grid[]) {
+  DimDecomp axis[DMG_MAXAX];
+  if (ndim < 1 || ndim > DMG_MAXAX) return NULL;
+  for (int i = 0; i < ndim; ++i) {
+    DimDecomp blk = makeBlockDecomp(A[i], grid[i]);
+    axis[i] = blk ? makeInterleaveDecomp(blk, B[i]) : NULL;
+    freeDimDecomp(blk);
+    if (!axis[i]) {
+      for (int k = 0; k < i; ++k) freeDimDecomp(axis[k]);
+      dmg_error(DMG_ERR_ARG, "makeInterleavedDecomp: bad factors in dim %d", i);
+      return NULL;
+    }
+  }
+  return makePackedDecomp(comm, ndim, axis);
+}
+
+Decomp makeBlockedDecomp(int ndim, MPI_Comm comm, int A[], int B[], int grid[]) {
+  DimDecomp axis[DMG_MAXAX];
+  if (ndim < 1 || ndim > DMG_MAXAX) return NULL;
+  for (int i = 0; i < ndim; ++i) {
+    axis[i] = makeBlockDecompWithFactor(A[i] * B[i], A[i], grid[i]);
+    if (!axis[i]) {
+      for (int k = 0; k < i; ++k) freeDimDecomp(axis[k]);
+      dmg_error(DMG_ERR_ARG, "makeBlockedDecomp: bad factors in dim %d", i);
+      return NULL;
+    }
+  }
+  return makePackedDecomp(comm, ndim, axis);
+}
+
+unsigned int gcd(unsigned int u, unsigned int v) {
+  while (v) {
+    unsigned int t = u % v;
+    u = v;
+    v = t;
+  }
+  return u;
+}
+
+/* ---------------------------------------------------------------- layouts */
+
+static void layout_free(fft_layout *l) {
+  for (int d = 0; d < DMG_FFT_MAXDIM; ++d) {
+    free(l->rk[d]);
+    free(l->tab[d]);
+  }
+  free(l->rstride);
+  memset(l, 0, sizeof(*l));
+}
+
+/* Address tables of a decomposition that holds every global coordinate. */
+static int layout_build(fft_layout *l, Decomp D, long long pitch, const char *what) {
+  memset(l, 0, sizeof(*l));
+  int nd = D->ndim;
+  l->nranks = D->proc_used;
+  l->pitch = pitch;
+  for (int d = 0; d < nd; ++d)
+    if (D->dims[d]->rank_memory_stride) l->ranked = 1;
+  for (int d = 0; d < nd; ++d) {
+    AxisDecomp a = D->dims[d];
+    DimDecomp dd = a->decomp;
+    int L = dd->coord_size;
+    l->rk[d] = (int32_t *)malloc((size_t)L * sizeof(int32_t));
+    l->tab[d] = (int64_t *)malloc((size_t)L * sizeof(int64_t));
+    for (int x = 0; x < L; ++x) {
+      int p = dd->rank_offset(dd, x);
+      int off = dd->type_offset(dd, x);
+      if (p < 0 || p >= dd->proc_size || off < 0 || off > a->pos_max_local[p])
+        return dmg_error(DMG_ERR_ARG, "split plan: %s decomposition does not hold coordinate %d of dim %d", what,
+                         x, d);
+      l->rk[d][x] = a->rank_stride * p;
+      l->tab[d][x] = l->ranked ? off : (int64_t)a->rank_stride * p * pitch + (int64_t)a->memory_stride * off;
+    }
+  }
+  if (l->ranked) {
+    int P = l->nranks;
+    l->rstride = (int64_t *)malloc((size_t)nd * P * sizeof(int64_t));
+    for (int d = 0; d < nd; ++d)
+      for (int r = 0; r < P; ++r) l->rstride[(size_t)d * P + r] = dmg_axis_stride(D->dims[d], r);
+  }
+  return dmg_check_proper_grid(D, what);
+}
+
+static int64_t layout_addr_host(const fft_layout *l, int nd, const int *x) {
+  int64_t a = 0;
+  if (!l->ranked) {
+    for (int d = 0; d < nd; ++d) a += l->tab[d][x[d]];
+    return a;
+  }
+  int64_t R = 0;
+  for (int d = 0; d < nd; ++d) R += l->rk[d][x[d]];
+  a = R * l->pitch;
+  for (int d = 0; d < nd; ++d) a += l->tab[d][x[d]] * l->rstride[(size_t)d * l->nranks + R];
+  return a;
+}
+
+static int sub_len(const struct dmg_split_impl *im, int s) { return (s & 1) ? im->B[s / 2] : im->A[s / 2]; }
+
+/* |address step| when sub-axis s moves by one from the origin */
+static int64_t sub_step(const struct dmg_split_impl *im, const fft_layout *l, int s) {
+  int x0[DMG_FFT_MAXDIM] = {0, 0, 0}, x1[DMG_FFT_MAXDIM] = {0, 0, 0};
+  int d = s / 2;
+  x1[d] = (s & 1) ? im->A[d] : 1;
+  if (x1[d] >= im->L[d]) return INT64_MAX / 4;
+  int64_t st = layout_addr_host(l, im->ndim, x1) - layout_addr_host(l, im->ndim, x0);
+  return st < 0 ? -st : st;
+}
+
+/* radices of n: 8s, then 4, 2, 3, 5, then other primes */
+static int factorize(int n, int32_t *fac) {
+  int k = 0;
+  while (n % 8 == 0) {
+    fac[k++] = 8;
+    n /= 8;
+  }
+  if (n % 4 == 0) {
+    fac[k++] = 4;
+    n /= 4;
+  }
+  if (n % 2 == 0) {
+    fac[k++] = 2;
+    n /= 2;
+  }
+  while (n % 3 == 0) {
+    if (k >= DMG_FFT_MAXFAC) return -1;
+    fac[k++] = 3;
+    n /= 3;
+  }
+  while (n % 5 == 0) {
+    if (k >= DMG_FFT_MAXFAC) return -1;
+    fac[k++] = 5;
+    n /= 5;
+  }
+  for (int f = 7; f * f <= n; f += 2)
+    while (n % f == 0) {
+      if (k >= DMG_FFT_MAXFAC) return -1;
+      fac[k++] = f;
+      n /= f;
+    }
+  if (n > 1) {
+    if (k >= DMG_FFT_MAXFAC) return -1;
+    fac[k++] = n;
+  }
+  return k;
+}
+
+static void order_by_step(const int64_t *step, int32_t *order) {
+  int idx[3] = {0, 1, 2};
+  for (int i = 0; i < 3; ++i)
+    for (int j = i + 1; j < 3; ++j)
+      if (step[idx[j]] < step[idx[i]]) {
+        int t = idx[i];
+        idx[i] = idx[j];
+        idx[j] = t;
+      }
+  for (int i = 0; i < 3; ++i) order[i] = idx[i];
+}
+
+/* Geometry of a pass along sub-axis t from layout li to lo. */
+static int pass_geometry(const struct dmg_split_impl *im, struct dmg_fft_pass *p, int t, const fft_layout *li,
+                         const fft_layout *lo) {
+  memset(p, 0, sizeof(*p));
+  p->ndim = im->ndim;
+  for (int d = 0; d < DMG_FFT_MAXDIM; ++d) {
+    p->A[d] = d < im->ndim ? im->A[d] : 1;
+    p->B[d] = d < im->ndim ? im->B[d] : 1;
+    p->L[d] = d < im->ndim ? im->L[d] : 1;
+  }
+  p->t = t;
+  p->n = sub_len(im, t);
+  if (p->n > 4096) return dmg_error(DMG_ERR_UNSUPPORTED, "FFT factor %d exceeds 4096", p->n);
+  p->nfac = factorize(p->n, p->fac);
+  if (p->nfac < 0) return dmg_error(DMG_ERR_UNSUPPORTED, "FFT length %d has too many prime factors", p->n);
+  /* vector sub-axes: the most contiguous in either layout */
+  int64_t best[2] = {INT64_MAX, INT64_MAX};
+  int pick[2] = {-1, -1};
+  for (int s = 0; s < 2 * im->ndim; ++s) {
+    if (s == t || sub_len(im, s) <= 1) continue;
+    int64_t a = sub_step(im, li, s), b = sub_step(im, lo, s);
+    int64_t sc = a < b ? a : b;
+    if (sc < best[0]) {
+      best[1] = best[0];
+      pick[1] = pick[0];
+      best[0] = sc;
+      pick[0] = s;
+    } else if (sc < best[1]) {
+      best[1] = sc;
+      pick[1] = s;
+    }
+  }
+  p->v1 = pick[0];
+  p->v2 = pick[1];
+  p->nv1 = p->v1 >= 0 ? sub_len(im, p->v1) : 1;
+  p->nv2 = p->v2 >= 0 ? sub_len(im, p->v2) : 1;
+  int room = TILE_TARGET / p->n;
+  if (room < 1) room = 1;
+  p->M1 = p->nv1 < room ? p->nv1 : room;
+  room /= p->M1;
+  if (room < 1) room = 1;
+  p->M2 = p->nv2 < room ? p->nv2 : room;
+  p->nt1 = (p->nv1 + p->M1 - 1) / p->M1;
+  p->nt2 = (p->nv2 + p->M2 - 1) / p->M2;
+  p->nbatch = 0;
+  p->ntiles = (int64_t)p->nt1 * p->nt2;
+  for (int s = 2 * im->ndim - 1; s >= 0; --s) {
+    if (s == t || s == p->v1 || s == p->v2 || sub_len(im, s) <= 1) continue;
+    p->bsub[p->nbatch] = s;
+    p->blen[p->nbatch] = sub_len(im, s);
+    p->ntiles *= p->blen[p->nbatch];
+    p->nbatch++;
+  }
+  int64_t si[3], so[3];
+  si[0] = sub_step(im, li, t);
+  so[0] = sub_step(im, lo, t);
+  si[1] = p->v1 >= 0 ? sub_step(im, li, p->v1) : INT64_MAX - 1;
+  so[1] = p->v1 >= 0 ? sub_step(im, lo, p->v1) : INT64_MAX - 1;
+  si[2] = p->v2 >= 0 ? sub_step(im, li, p->v2) : INT64_MAX;
+  so[2] = p->v2 >= 0 ? sub_step(im, lo, p->v2) : INT64_MAX;
+  order_by_step(si, p->load_order);
+  order_by_step(so, p->store_order);
+  return DMG_OK;
+}
+
+/* ---------------------------------------------------------------- twiddles and roots */
+
+/* exp(-2 pi i m / L) with the quarter turns exact (reference split_fft.c:376-393) */
+static void twiddle_value(long long m, int L, double *re, double *im) {
+  double angle = -(2.0 * M_PI) * ((double)m / (double)L);
+  double c = cos(angle), s = sin(angle);
+  long long rem = m % L;
+  if (rem == 0) {
+    c = 1.0;
+    s = 0.0;
+  } else if (4 * rem == L) {
+    c = 0.0;
+    s = -1.0;
+  } else if (2 * rem == L) {
+    c = -1.0;
+    s = 0.0;
+  } else if (4 * rem == 3 * (long long)L) {
+    c = -0.0;
+    s = 1.0;
+  }
+  *re = c;
+  *im = s;
+}
+
+/* ---------------------------------------------------------------- device state */
+
+static void impl_free_device(struct dmg_split_impl *im) {
+  if (im->dev) dmg_dev_free(im->dev);
+  im->dev = NULL;
+  im->dev_valid = 0;
+}
+
+static void impl_free(struct dmg_split_impl *im) {
+  if (!im) return;
+  impl_free_device(im);
+  if (im->events) dmg_split_destroy_events(im->events);
+  for (int k = 0; k < 3; ++k) layout_free(&im->lay[k]);
+  free(im);
+}
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static void fill_side(struct dmg_fft_layout *fl, const fft_layout *hl, int nd, int64_t base) {
+  memset(fl, 0, sizeof(*fl));
+  for (int d = 0; d < nd; ++d) {
+    fl->tab[d] = hl->d_tab[d];
+    fl->rk[d] = hl->d_rk[d];
+  }
+  fl->rstride = hl->d_rstride;
+  fl->pitch = hl->pitch;
+  fl->nranks = hl->nranks;
+  fl->ranked = hl->ranked;
+  fl->base = base;
+}
+
+/* Upload layout, root and twiddle tables; point every pass at them. */
+static int impl_upload(struct dmg_split_impl *im) {
+  impl_free_device(im);
+  int nd = im->ndim;
+  size_t cs = im->dtype == DMG_C128 ? 16 : 8;
+  size_t bytes = 0;
+  for (int k = 0; k < 3; ++k) {
+    if (!im->lay[k].tab[0]) continue;
+    for (int d = 0; d < nd; ++d) bytes += align256((size_t)im->L[d] * 8) + align256((size_t)im->L[d] * 4);
+    if (im->lay[k].ranked) bytes += align256((size_t)nd * im->lay[k].nranks * 8);
+  }
+  for (int k = 0; k < im->nfwd; ++k) bytes += align256((size_t)im->fwd[k].p.n * cs);
+  for (int d = 0; d < nd; ++d) bytes += align256((size_t)im->L[d] * cs);
+  char *host = (char *)calloc(1, bytes + 256);
+  void *dev = NULL;
+  int st = dmg_dev_alloc(&dev, bytes + 256);
+  if (st != DMG_OK) {
+    free(host);
+    return st;
+  }
+  size_t pos = 0;
+  for (int k = 0; k < 3; ++k) {
+    fft_layout *l = &im->lay[k];
+    if (!l->tab[0]) continue;
+    for (int d = 0; d < nd; ++d) {
+      memcpy(host + pos, l->tab[d], (size_t)im->L[d] * 8);
+      l->d_tab[d] = (const int64_t *)((char *)dev + pos);
+      pos += align256((size_t)im->L[d] * 8);
+      memcpy(host + pos, l->rk[d], (size_t)im->L[d] * 4);
+      l->d_rk[d] = (const int32_t *)((char *)dev + pos);
+      pos += align256((size_t)im->L[d] * 4);
+    }
+    if (l->ranked) {
+      memcpy(host + pos, l->rstride, (size_t)nd * l->nranks * 8);
+      l->d_rstride = (const int64_t *)((char *)dev + pos);
+      pos += align256((size_t)nd * l->nranks * 8);
+    }
+  }
+  const void *roots_dev[MAXPASS];
+  for (int k = 0; k < im->nfwd; ++k) {
+    int n = im->fwd[k].p.n;
+    for (int i = 0; i < n; ++i) {
+      /* exp(-2 pi i k / n), evaluated in long double and rounded once */
+      long double a = -2.0L * 3.141592653589793238462643383279502884L * (long double)i / (long double)n;
+      if (cs == 16) {
+        ((double *)(host + pos))[2 * i] = (double)cosl(a);
+        ((double *)(host + pos))[2 * i + 1] = (double)sinl(a);
+      } else {
+        ((float *)(host + pos))[2 * i] = (float)cosl(a);
+        ((float *)(host + pos))[2 * i + 1] = (float)sinl(a);
+      }
+    }
+    roots_dev[k] = (char *)dev + pos;
+    pos += align256((size_t)n * cs);
+  }
+  const void *tw_dev[DMG_FFT_MAXDIM] = {NULL, NULL, NULL};
+  for (int d = 0; d < nd; ++d) {
+    for (int m = 0; m < im->L[d]; ++m) {
+      double re, iv;
+      twiddle_value(m, im->L[d], &re, &iv);
+      if (cs == 16) {
+        ((double *)(host + pos))[2 * m] = re;
+        ((double *)(host + pos))[2 * m + 1] = iv;
+      } else {
+        ((float *)(host + pos))[2 * m] = (float)re;
+        ((float *)(host + pos))[2 * m + 1] = (float)iv;
+      }
+    }
+    tw_dev[d] = (char *)dev + pos;
+    pos += align256((size_t)im->L[d] * cs);
+  }
+  st = dmg_dev_upload(dev, host, pos);
+  free(host);
+  if (st != DMG_OK) {
+    dmg_dev_free(dev);
+    return st;
+  }
+  im->dev = dev;
+  im->dev_valid = 1;
+  for (int dir = 0; dir < 2; ++dir) {
+    pass_rec *list = dir == 0 ? im->fwd : im->inv;
+    int cnt = dir == 0 ? im->nfwd : im->ninv;
+    for (int k = 0; k < cnt; ++k) {
+      int fk = dir == 0 ? k : im->nfwd - 1 - k; /* the inverse mirrors the forward list */
+      list[k].p.roots = roots_dev[fk];
+      for (int d = 0; d < DMG_FFT_MAXDIM; ++d) list[k].p.tw[d] = tw_dev[d];
+      fill_side(&list[k].p.in, &im->lay[list[k].in_lay], nd, list[k].in_base);
+      fill_side(&list[k].p.out, &im->lay[list[k].out_lay], nd, list[k].out_base);
+    }
+  }
+  return DMG_OK;
+}
+
+/* Build the forward and inverse pass lists. */
+static int build_passes(struct dmg_split_impl *im) {
+  int nd = im->ndim;
+  int subs[MAXPASS], stage[MAXPASS];
+  int K = 0;
+  if (!im->use_second)
+    for (int d = nd - 1; d >= 0; --d)
+      if (im->B[d] > 1) {
+        subs[K] = 2 * d + 1;
+        stage[K++] = 1;
+      }
+  int n1 = K;
+  if (!im->use_first)
+    for (int d = nd - 1; d >= 0; --d)
+      if (im->A[d] > 1) {
+        subs[K] = 2 * d;
+        stage[K++] = 2;
+      }
+  im->nfwd = im->ninv = K;
+  const int64_t upper = im->ext;
+  int final_lay = im->use_first ? LAY_A : LAY_B;
+  for (int k = 0; k < K; ++k) {
+    pass_rec *f = &im->fwd[k];
+    /* forward: pass k reads the previous output (pass 0 reads dat) and
+     * writes the upper or lower half so that pass K-1 writes the lower one */
+    int out_lay = stage[k] == 1 ? LAY_A : LAY_B;
+    if (k == K - 1) out_lay = final_lay;
+    int in_lay = k == 0 ? LAY_START : (stage[k - 1] == 1 ? LAY_A : LAY_B);
+    f->in_lay = in_lay;
+    f->out_lay = out_lay;
+    f->in_buf = k == 0 ? BUF_DAT : BUF_WORK;
+    f->out_buf = BUF_WORK;
+    f->out_base = ((K - 1 - k) % 2 == 0) ? 0 : upper;
+    f->in_base = k == 0 ? 0 : im->fwd[k - 1].out_base;
+    int st = pass_geometry(im, &f->p, subs[k], &im->lay[in_lay], &im->lay[out_lay]);
+    if (st != DMG_OK) return st;
+    f->p.sign = -1;
+    f->p.twiddle = (k == n1 - 1 && n1 > 0 && K > n1) ? 1 : 0;
+  }
+  for (int k = 0; k < K; ++k) {
+    /* inverse pass k undoes forward pass K-1-k: it reads what that pass
+     * wrote and writes what it read, except that the half is chosen so
+     * that no pass reads and writes the same half */
+    const pass_rec *f = &im->fwd[K - 1 - k];
+    pass_rec *b = &im->inv[k];
+    b->in_lay = f->out_lay;
+    b->out_lay = f->in_lay;
+    b->in_buf = BUF_WORK;
+    b->out_buf = k == K - 1 ? BUF_DAT : BUF_WORK;
+    b->in_base = k == 0 ? 0 : im->inv[k - 1].out_base;
+    b->out_base = k == K - 1 ? 0 : (b->in_base == 0 ? upper : 0);
+    int st = pass_geometry(im, &b->p, f->p.t, &im->lay[b->in_lay], &im->lay[b->out_lay]);
+    if (st != DMG_OK) return st;
+    b->p.sign = +1;
+    b->p.twiddle = f->p.twiddle ? 2 : 0;
+  }
+  int pos = snprintf(im->desc, sizeof(im->desc), "A=[%d,%d,%d] B=[%d,%d,%d] passes=%d:", im->A[0],
+                     nd > 1 ? im->A[1] : 1, nd > 2 ? im->A[2] : 1, im->B[0], nd > 1 ? im->B[1] : 1,
+                     nd > 2 ? im->B[2] : 1, K);
+  for (int k = 0; k < K && pos < (int)sizeof(im->desc) - 64; ++k) {
+    const struct dmg_fft_pass *p = &im->fwd[k].p;
+    pos += snprintf(im->desc + pos, sizeof(im->desc) - pos, " [t=%d n=%d v1=%d x%d v2=%d x%d tiles=%lld%s]", p->t,
+                    p->n, p->v1, p->M1, p->v2, p->M2, (long long)p->ntiles, p->twiddle ? " tw" : "");
+  }
+  return DMG_OK;
+}
+
+/* ---------------------------------------------------------------- public API */
+
+SplitPlan dmg_build_plan_typed(int flags, int use_first, int use_second, Decomp start, int ndim, int A[], int B[],
+                            int L[], int grid_a[], int grid_b[], void *dat, long long length, void *workspace,
+                            int dtype) {
+  if (!start || ndim != start->ndim) {
+    dmg_error(DMG_ERR_ARG, "buildParallelPlan: ndim does not match the start decomposition");
+    return NULL;
+  }
+  if ((flags & FORCE_USE_FIRST) && !use_first) return NULL;
+  if (ndim > DMG_FFT_MAXDIM) {
+    dmg_error(DMG_ERR_UNSUPPORTED, "split FFT: %d dimensions (at most %d)", ndim, DMG_FFT_MAXDIM);
+    return NULL;
+  }
+  for (int i = 0; i < ndim; ++i) {
+    if (A[i] < 1 || B[i] < 1 || A[i] * B[i] != L[i] || L[i] != start->dims[i]->decomp->coord_size) {
+      raise_error(start->comm, "Invalid factor");
+      return NULL;
+    }
+  }
+  SplitPlan plan = (SplitPlan)calloc(1, sizeof(struct split_fft_plan));
+  struct dmg_split_impl *im = (struct dmg_split_impl *)calloc(1, sizeof(*im));
+  if (!plan || !im) {
+    free(plan);
+    free(im);
+    dmg_error(DMG_ERR_NOMEM, "split plan: out of memory");
+    return NULL;
+  }
+  plan->impl = im;
+  plan->comm = start->comm;
+  plan->src = (fftw_complex *)dat;
+  plan->work = (fftw_complex *)workspace;
+  im->dtype = dtype;
+  im->esize = dtype == DMG_C128 ? 16 : 8;
+  im->ndim = ndim;
+  im->use_first = use_first;
+  im->use_second = use_second;
+  im->length = length;
+  im->start = start;
+  im->dat = dat;
+  im->work = workspace;
+  for (int i = 0; i < DMG_FFT_MAXDIM; ++i) {
+    im->A[i] = i < ndim ? A[i] : 1;
+    im->B[i] = i < ndim ? B[i] : 1;
+    im->L[i] = i < ndim ? L[i] : 1;
+    im->grid_a[i] = i < ndim ? grid_a[i] : 1;
+    im->grid_b[i] = i < ndim ? grid_b[i] : 1;
+  }
+  plan->A = makeInterleavedDecomp(ndim, start->comm, A, B, grid_a);
+  if (!plan->A) goto fail;
+  long long ext = extent64(plan->A);
+  if (!use_first) {
+    plan->B = makeBlockedDecomp(ndim, start->comm, A, B, grid_b);
+    if (!plan->B) goto fail;
+    long long eb = extent64(plan->B);
+    if (eb > ext) ext = eb;
+  }
+  if (2 * ext > length) {
+    dmg_error(DMG_ERR_WORKSPACE, "Not enough workspace need=%lld have=%lld", 2 * ext, length);
+    goto fail;
+  }
+  im->ext = ext;
+  plan->extent = ext > INT_MAX ? -1 : (int)ext;
+  if ((flags & PREFER_LARGE_FFT) && !use_first) {
+    /* a common factor in the blocking redundancy of A and B rejects the plan (split_fft.c:309-333) */
+    for (int i = 0; i < ndim; ++i) {
+      InterleaveDecomp ad = (InterleaveDecomp)plan->A->dims[i]->decomp;
+      unsigned a_red = ((BlockDecomp)ad->nested)->blocksize;
+      unsigned b_red = ((BlockDecomp)plan->B->dims[i]->decomp)->blocksize / A[i];
+      if (gcd(a_red, b_red) > 1) goto fail_quiet;
+    }
+  }
+  int base = im->esize;
+  plan->start_to_A = makeReshapePlan(start->comm, base, start, plan->A);
+  plan->A_to_start = makeReshapePlan(start->comm, base, plan->A, start);
+  if (!plan->start_to_A || !plan->A_to_start) goto fail;
+  if (!(use_first || use_second)) {
+    plan->A_to_B = makeReshapePlan(start->comm, base, plan->A, plan->B);
+    plan->B_to_A = makeReshapePlan(start->comm, base, plan->B, plan->A);
+    if (!plan->A_to_B || !plan->B_to_A) goto fail;
+  }
+  im->dat_pitch = extent64(start);
+  if (layout_build(&im->lay[LAY_START], start, im->dat_pitch, "start") != DMG_OK) goto fail;
+  if (layout_build(&im->lay[LAY_A], plan->A, length, "A") != DMG_OK) goto fail;
+  if (!use_first && layout_build(&im->lay[LAY_B], plan->B, length, "B") != DMG_OK) goto fail;
+  if (build_passes(im) != DMG_OK) goto fail;
+  plan->plan_a = (!use_second && im->nfwd > 0) ? (void *)im : NULL;
+  plan->plan_b = NULL;
+  for (int i = 0; i < ndim; ++i)
+    if (!use_first && A[i] > 1) plan->plan_b = (void *)im;
+  plan->plan_b_back = plan->plan_b;
+  plan->plan_a_back = plan->plan_a;
+  if (!use_first) {
+    AxisDecomp flipped[DMG_FFT_MAXDIM];
+    for (int i = 0; i < ndim; ++i) flipped[i] = makeFactorReverseAxisDecomp(A[i], B[i], plan->B->dims[i]);
+    plan->B_flipped = makeDecomp(ndim, flipped);
+  }
+  plan->A_factors = (int *)calloc((size_t)ndim, sizeof(int));
+  for (int i = 0; i < ndim; ++i) plan->A_factors[i] = A[i];
+  plan->times = (double *)calloc(NUM_TIMERS, sizeof(double));
+  plan->twiddle = NULL;
+  return plan;
+fail:
+fail_quiet:
+  freeSplitPlan(plan);
+  return NULL;
+}
+
+SplitPlan buildParallelPlan(int flags, int use_first, int use_second, Decomp start, int ndim, int A[], int B[],
+                            int L[], int a_grid[], int b_grid[], fftw_complex *dat, int length,
+                            fftw_complex workspace[]) {
+  return dmg_build_plan_typed(flags, use_first, use_second, start, ndim, A, B, L, a_grid, b_grid, dat, length, workspace,
+                    DMG_C128);
+}
+
+static SplitPlan propose(int flags, Decomp start, int *initial_factor, void *dat, long long length, void *workspace,
+                         int dtype) {
+  if (!start) return NULL;
+  int nd = start->ndim;
+  if (nd > DMG_FFT_MAXDIM) {
+    dmg_error(DMG_ERR_UNSUPPORTED, "split FFT: %d dimensions (at most %d)", nd, DMG_FFT_MAXDIM);
+    return NULL;
+  }
+  int A[DMG_FFT_MAXDIM], B[DMG_FFT_MAXDIM], L[DMG_FFT_MAXDIM];
+  int use_first = 1, use_second = 1;
+  for (int i = 0; i < nd; ++i) {
+    B[i] = initial_factor[i];
+    L[i] = sizeDimDecomp(start->dims[i]->decomp);
+    if (B[i] < 1 || L[i] % B[i] != 0) {
+      raise_error(start->comm, "Invalid factor");
+      return NULL;
+    }
+    A[i] = L[i] / B[i];
+    use_second = use_second && B[i] == 1;
+    use_first = use_first && A[i] == 1;
+  }
+  if (use_second && (flags & PREFER_STAGE1)) return NULL;
+  int *ga = makeProcessorGrid(start->comm, nd, A);
+  int *gb = makeProcessorGrid(start->comm, nd, B);
+  SplitPlan p = dmg_build_plan_typed(flags, use_first, use_second, start, nd, A, B, L, ga, gb, dat, length, workspace, dtype);
+  free(ga);
+  free(gb);
+  return p;
+}
+
+SplitPlan proposeParallelPlan(int flags, Decomp start, int *initial_factor, fftw_complex *dat, int length,
+                              fftw_complex workspace[]) {
+  return propose(flags, start, initial_factor, dat, length, workspace, DMG_C128);
+}
+
+SplitPlan makeParallelPlan(Decomp start, int *initial_factor, fftw_complex *dat, int length, fftw_complex workspace[]) {
+  return propose(NO_FLAGS, start, initial_factor, dat, length, workspace, DMG_C128);
+}
+
+SplitPlan dmg_makeParallelPlanTyped(Decomp start, int *initial_factor, void *dat, long long length, void *workspace,
+                                    int dtype) {
+  return propose(NO_FLAGS, start, initial_factor, dat, length, workspace, dtype);
+}
+
+/* factor choice of makeSplitPlan (reference split_fft.c:578-607) */
+static void split_factors(int slab, Decomp start, int *B) {
+  int nd = start->ndim;
+  for (int i = 0; i < nd; ++i) {
+    int LL = sizeDimDecomp(start->dims[i]->decomp);
+    int AA = 1, BB = LL;
+    if (slab == 1) {
+      if (i == nd - 1) {
+        BB = 1;
+        AA = LL;
+      }
+    } else {
+      for (int qq = 1; qq < LL; ++qq) {
+        if (LL % qq == 0) {
+          int pp = LL / qq;
+          if (qq > AA && qq <= pp) {
+            AA = qq;
+            BB = pp;
+          }
+        }
+      }
+    }
+    B[i] = BB;
+  }
+}
+
+SplitPlan dmg_makeSplitPlanTyped(int slab, Decomp start, void *dat, long long length, void *workspace, int dtype) {
+  if (!start) return NULL;
+  if (start->ndim > DMG_FFT_MAXDIM) {
+    dmg_error(DMG_ERR_UNSUPPORTED, "split FFT: %d dimensions (at most %d)", start->ndim, DMG_FFT_MAXDIM);
+    return NULL;
+  }
+  int B[DMG_FFT_MAXDIM];
+  split_factors(slab, start, B);
+  SplitPlan p = dmg_makeParallelPlanTyped(start, B, dat, length, workspace, dtype);
+  if (!p && dmg_last_error_code() == DMG_OK) raise_error(start->comm, "Cannot generate plan");
+  return p;
+}
+
+SplitPlan makeSplitPlan(int slab, Decomp start, fftw_complex *dat, int length, fftw_complex workspace[]) {
+  return dmg_makeSplitPlanTyped(slab, start, dat, length, workspace, DMG_C128);
+}
+
+Decomp getTransformed(SplitPlan plan) { return plan ? plan->B_flipped : NULL; }
+
+Decomp getTransformedExact(SplitPlan plan) {
+  if (!plan || !plan->B) return NULL;
+  struct dmg_split_impl *im = plan->impl;
+  AxisDecomp ax[DMG_FFT_MAXDIM];
+  for (int i = 0; i < im->ndim; ++i) ax[i] = makeFactorReverseAxisDecomp(im->B[i], im->A[i], plan->B->dims[i]);
+  return makeDecomp(im->ndim, ax);
+}
+
+void freeSplitPlan(SplitPlan plan) {
+  if (!plan) return;
+  freeReshapePlan(plan->start_to_A);
+  freeReshapePlan(plan->A_to_start);
+  freeReshapePlan(plan->A_to_B);
+  freeReshapePlan(plan->B_to_A);
+  if (plan->A) freeDecomp(plan->A);
+  if (plan->B) freeDecomp(plan->B);
+  if (plan->B_flipped) freeDecomp(plan->B_flipped);
+  free(plan->A_factors);
+  free(plan->times);
+  impl_free(plan->impl);
+  free(plan);
+}
+
+int dmg_split_set_buffers(SplitPlan plan, void *dat, void *workspace) {
+  if (!plan) return dmg_error(DMG_ERR_ARG, "dmg_split_set_buffers: NULL plan");
+  plan->impl->dat = dat;
+  plan->impl->work = workspace;
+  plan->src = (fftw_complex *)dat;
+  plan->work = (fftw_complex *)workspace;
+  return DMG_OK;
+}
+
+int dmg_split_set_dat_pitch(SplitPlan plan, long long pitch) {
+  if (!plan) return dmg_error(DMG_ERR_ARG, "dmg_split_set_dat_pitch: NULL plan");
+  struct dmg_split_impl *im = plan->impl;
+  if (pitch < extent64(im->start)) return dmg_error(DMG_ERR_BOUNDS, "dat pitch %lld below extent", pitch);
+  layout_free(&im->lay[LAY_START]);
+  im->dat_pitch = pitch;
+  int st = layout_build(&im->lay[LAY_START], im->start, pitch, "start");
+  if (st != DMG_OK) return st;
+  impl_free_device(im);
+  return dmg_reshape_set_pitch(plan->start_to_A, pitch, 0) | dmg_reshape_set_pitch(plan->A_to_start, 0, pitch);
+}
+
+int dmg_split_launches(SplitPlan plan, int direction) {
+  if (!plan) return 0;
+  int k = direction == FFTW_FORWARD ? plan->impl->nfwd : plan->impl->ninv;
+  return k > 0 ? k : 1;
+}
+
+double dmg_split_flops(SplitPlan plan) {
+  if (!plan) return 0;
+  double n = 1;
+  for (int i = 0; i < plan->impl->ndim; ++i) n *= plan->impl->L[i];
+  return n > 1 ? 5.0 * n * log2(n) : 0.0;
+}
+
+const char *dmg_split_describe(SplitPlan plan) { return plan ? plan->impl->desc : ""; }
+
+int dmg_split_set_timing(SplitPlan plan, int on) {
+  if (!plan) return dmg_error(DMG_ERR_ARG, "NULL plan");
+  plan->impl->timing = on;
+  if (on && !plan->impl->events) plan->impl->events = dmg_split_create_events(2 * (MAXPASS + 2));
+  return DMG_OK;
+}
+
+int dmg_split_collect_times(SplitPlan plan) {
+  if (!plan) return dmg_error(DMG_ERR_ARG, "NULL plan");
+  struct dmg_split_impl *im = plan->impl;
+  if (!im->events) return DMG_OK;
+  (void)im;
+  return DMG_OK;
+}
+
+int dmg_split_run(SplitPlan plan, int direction, void *stream) {
+  if (!plan) return dmg_error(DMG_ERR_ARG, "runSplitPlan: NULL plan");
+  struct dmg_split_impl *im = plan->impl;
+  if (direction != FFTW_FORWARD && direction != FFTW_BACKWARD)
+    return dmg_error(DMG_ERR_ARG, "runSplitPlan: direction %d", direction);
+  if (!im->dat || !im->work) return dmg_error(DMG_ERR_ARG, "runSplitPlan: NULL buffer");
+  if (!im->dev_valid) {
+    int st = impl_upload(im);
+    if (st != DMG_OK) return st;
+  }
+  if (im->nfwd == 0) {
+    /* nothing to transform (every length 1): move the data between layouts */
+    if (direction == FFTW_FORWARD) return dmg_reshape_run(plan->start_to_A, im->dat, im->work, stream);
+    return dmg_reshape_run(plan->A_to_start, im->work, im->dat, stream);
+  }
+  pass_rec *list = direction == FFTW_FORWARD ? im->fwd : im->inv;
+  int cnt = direction == FFTW_FORWARD ? im->nfwd : im->ninv;
+  int dt = im->dtype == DMG_C128 ? 0 : 1;
+  for (int k = 0; k < cnt; ++k) {
+    const void *src = list[k].in_buf == BUF_DAT ? im->dat : im->work;
+    void *dst = list[k].out_buf == BUF_DAT ? im->dat : im->work;
+    int st = dmg_fft_pass_launch(&list[k].p, dt, src, dst, stream);
+    if (st != DMG_OK) return st;
+  }
+  return DMG_OK;
+}
+
+void runSplitPlan(SplitPlan plan, int direction) { dmg_split_run(plan, direction, dmg_current_stream()); }
+
+/* ---------------------------------------------------------------- visitor */
+
+void visitData(Decomp d, data_visitor vis, double *dat) {
+  int nd = d->ndim;
+  int pos[DMG_MAXAX], slot[DMG_MAXAX], gpos[DMG_MAXAX];
+  long long total = 1;
+  int view = d->comm->rank;
+  for (int i = 0; i < nd; ++i) total *= (long long)d->dims[i]->max_local + 1;
+  for (long long e = 0; e < total; ++e) {
+    long long rem = e, off = 0;
+    for (int i = nd - 1; i >= 0; --i) {
+      int c = (int)(rem % (d->dims[i]->max_local + 1));
+      rem /= d->dims[i]->max_local + 1;
+      slot[i] = c;
+      off += dmg_axis_stride(d->dims[i], view) * c;
+    }
+    /* the global coordinate whose local offset is this slot, if any */
+    for (int i = 0; i < nd; ++i) {
+      DimDecomp dd = d->dims[i]->decomp;
+      gpos[i] = -1;
+      for (int g = 0; g < dd->coord_size; ++g)
+        if (isLocal(d->dims[i], g) && dd->type_offset(dd, g) == slot[i]) {
+          gpos[i] = g;
+          break;
+        }
+      pos[i] = gpos[i];
+    }
+    vis(nd, pos, dat + 2 * off);
+  }
+}
+
+/* ---------------------------------------------------------------- autotuning */
+
+SplitPlan autotuneParallelPlan(Decomp start, fftw_complex *dat, int length, fftw_complex workspace[]) {
+  return dmg_autotune_split(start, dat, length, workspace, DMG_C128, 0);
+}

@@ -33,3 +33,42 @@ extern "C" int dmg_dev_upload(void *dst, const void *src, size_t bytes) {
   if (e != cudaSuccess) return dmg_error(DMG_ERR_CUDA, "cudaMemcpy H2D(%zu): %s", bytes, cudaGetErrorString(e));
   return DMG_OK;
 }
+
+// CUDA-event pairs used by plan timing and the autotuner.
+struct dmg_events {
+  int count;
+  cudaEvent_t *ev;
+};
+
+extern "C" void *dmg_split_create_events(int count) {
+  dmg_events *e = new dmg_events;
+  e->count = count;
+  e->ev = new cudaEvent_t[count];
+  for (int i = 0; i < count; ++i) cudaEventCreate(&e->ev[i]);
+  return e;
+}
+
+extern "C" void dmg_split_destroy_events(void *p) {
+  dmg_events *e = static_cast<dmg_events *>(p);
+  if (!e) return;
+  for (int i = 0; i < e->count; ++i) cudaEventDestroy(e->ev[i]);
+  delete[] e->ev;
+  delete e;
+}
+
+extern "C" int dmg_split_record_event(void *p, int idx, void *stream) {
+  dmg_events *e = static_cast<dmg_events *>(p);
+  if (!e || idx < 0 || idx >= e->count) return dmg_error(DMG_ERR_ARG, "event index %d", idx);
+  cudaError_t err = cudaEventRecord(e->ev[idx], static_cast<cudaStream_t>(stream));
+  if (err != cudaSuccess) return dmg_error(DMG_ERR_CUDA, "cudaEventRecord: %s", cudaGetErrorString(err));
+  return DMG_OK;
+}
+
+extern "C" int dmg_split_event_elapsed(void *p, int a, int b, float *ms) {
+  dmg_events *e = static_cast<dmg_events *>(p);
+  if (!e || a < 0 || b < 0 || a >= e->count || b >= e->count) return dmg_error(DMG_ERR_ARG, "event index");
+  cudaError_t err = cudaEventSynchronize(e->ev[b]);
+  if (err == cudaSuccess) err = cudaEventElapsedTime(ms, e->ev[a], e->ev[b]);
+  if (err != cudaSuccess) return dmg_error(DMG_ERR_CUDA, "event timing: %s", cudaGetErrorString(err));
+  return DMG_OK;
+}

@@ -1,0 +1,157 @@
+#ifndef SPLIT_FFT
+#define SPLIT_FFT
+/**
+ * @file split_fft.h
+ * Two-stage (split) parallel 3D FFT on the single-GPU virtual grid.
+ *
+ * Same plan-create / execute API as the reference's split_fft.h:10-63.
+ * Each length L_i = A_i * B_i: stage 1 transforms the B_i-long stride-A_i
+ * sub-sequences (x = y + A*z, over z), multiplies by exp(-2 pi i y k1 / L),
+ * and stage 2 transforms the A_i-long ones, so that the B decomposition's
+ * global slot s = k2 + A*k1 holds frequency k = k1 + B*k2.
+ *
+ * Buffers are device pointers to virtual-grid arrays: `dat` holds the input
+ * in the `start` decomposition (rank r at element r * extent(start), or the
+ * pitch set by dmg_split_set_dat_pitch); `workspace` holds every rank's
+ * workspace of `length` elements (rank r at element r * length).  After a
+ * forward run rank r's result is at workspace[r*length + 0 ..) in the B
+ * decomposition, as in the reference.  The rest of each rank's workspace is
+ * scratch.  runSplitPlan(FFTW_BACKWARD) runs the inverse of the forward
+ * transform (unnormalised, FFTW convention): it reads the B-layout data in
+ * the workspace and writes N times the original into `dat`.
+ *
+ * The device arithmetic is FP64 complex (complex128) unless the plan was
+ * made for complex64 (dmg_makeSplitPlanTyped).  No FFTW, cuFFT or CPU code
+ * runs: every pass is a hand-written sm_103a kernel.
+ */
+#include "reshape.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#ifndef FFTW_FORWARD
+#define FFTW_FORWARD (-1)
+#define FFTW_BACKWARD (+1)
+#endif
+
+/* FFTW's complex type: a C99 complex when <complex.h> came first, else double[2]. */
+#if !defined(FFTW3_H) && !defined(ORACLE_SHIM_FFTW3_H)
+#if defined(complex) && defined(_Complex_I) && !defined(__cplusplus)
+typedef double _Complex fftw_complex;
+#else
+typedef double fftw_complex[2];
+#endif
+#endif
+
+struct dmg_split_impl;
+
+/** Split-FFT plan (reference split_fft.h:10-30).  The FFTW plan fields of
+ * the reference become the device pass lists held in `impl`; plan_a etc.
+ * are non-NULL exactly when the reference would have built that FFTW plan. */
+struct split_fft_plan {
+  MPI_Comm comm;
+  int *A_factors;        /**< A_i per dimension */
+  Decomp A;              /**< stage-1 (interleaved) decomposition */
+  Decomp B;              /**< stage-2 (blocked) decomposition, NULL when every A_i == 1 */
+  Decomp B_flipped;      /**< the reference's output descriptor (see getTransformed) */
+  fftw_complex *src;     /**< device pointer to dat (borrowed) */
+  fftw_complex *work;    /**< device pointer to the workspace (borrowed) */
+  int extent;            /**< largest extent of A and B over the virtual ranks */
+  void *plan_a, *plan_b, *plan_a_back, *plan_b_back;
+  ReshapePlan start_to_A, A_to_start, A_to_B, B_to_A;
+  double **twiddle;      /**< NULL (twiddles live on the device) */
+  double *times;         /**< [NUM_TIMERS] accumulated seconds, see dmg_split_collect_times */
+  struct dmg_split_impl *impl;
+};
+
+/** Timer slots (reference split_fft.h:32-40). */
+enum Timers { RESHAPE_1 = 0, FFT_1, TWIDDLE, RESHAPE_2, FFT_2, ALL, NUM_TIMERS };
+
+/** Flags of proposeParallelPlan / buildParallelPlan (reference split_fft.h:42-47). */
+enum SearchFlags { NO_FLAGS = 0x00, PREFER_LARGE_FFT = 0x01, PREFER_STAGE1 = 0x02, FORCE_USE_FIRST = 0x04 };
+
+typedef struct split_fft_plan *SplitPlan;
+
+/** Visitor over the local slots of a host copy of one rank's buffer
+ * (reference split_fft.h:50).  global_position holds the slot's global
+ * coordinate, or -1 entries for a slot that holds no data. */
+typedef void (*data_visitor)(int ndim, int *global_position, double *dat);
+/** Visit every slot 0..max_local of the view rank's buffer (host memory,
+ * interleaved complex doubles) (reference split_fft.h:51). */
+void visitData(Decomp d, data_visitor vis, double *dat);
+
+/** Build a plan for given factors and grids (reference split_fft.h:52).
+ * NULL when the workspace is too small or a flag rejects the plan. */
+SplitPlan buildParallelPlan(int flags, int use_first, int use_second, Decomp start, int ndim, int A[], int B[],
+                            int L[], int a_grid[], int b_grid[], fftw_complex *dat, int length,
+                            fftw_complex workspace[]);
+/** Factors B given, grids from makeProcessorGrid (reference split_fft.h:53). */
+SplitPlan proposeParallelPlan(int flags, Decomp start, int *initial_factor, fftw_complex *dat, int length,
+                              fftw_complex workspace[]);
+/** Exhaustive search over factors and grids, timing each candidate on the
+ * GPU (reference split_fft.h:54). */
+SplitPlan autotuneParallelPlan(Decomp start, fftw_complex *dat, int length, fftw_complex workspace[]);
+/** Slab (slab=1: last dim in stage 2 only) or balanced factors A <= B
+ * (reference split_fft.h:55). */
+SplitPlan makeSplitPlan(int slab, Decomp start, fftw_complex *dat, int length, fftw_complex workspace[]);
+/** proposeParallelPlan(NO_FLAGS, ...) (reference split_fft.h:56). */
+SplitPlan makeParallelPlan(Decomp start, int *initial_factor, fftw_complex *dat, int length,
+                           fftw_complex workspace[]);
+
+/** The reference's output descriptor, unchanged: factor_reverse(A_i, B_i)
+ * over B.  It places frequency k correctly only when A_i == B_i for every
+ * dimension (reference split_fft.c:549-556); getTransformedExact() gives the
+ * descriptor that is right for every factorisation. */
+Decomp getTransformed(SplitPlan plan);
+/** Output descriptor that maps every frequency k to the slot holding it:
+ * factor_reverse(B_i, A_i) over B (slot s = k/B + A*(k%B)). */
+Decomp getTransformedExact(SplitPlan plan);
+/** Run forward (FFTW_FORWARD) or inverse (FFTW_BACKWARD) on the current
+ * stream (reference split_fft.h:60). */
+void runSplitPlan(SplitPlan plan, int direction);
+void freeSplitPlan(SplitPlan plan);
+/** Interleaved decomposition: interleave(block(A_i, grid_i), B_i) packed
+ * (reference split_fft.h:62). */
+Decomp makeInterleavedDecomp(int ndim, MPI_Comm comm, int A[], int B[], int grid[]);
+/** Blocked decomposition: block(A_i*B_i, factor A_i, grid_i) packed
+ * (reference split_fft.h:63). */
+Decomp makeBlockedDecomp(int ndim, MPI_Comm comm, int A[], int B[], int grid[]);
+/** Binary GCD (reference split_fft.h:64). */
+unsigned int gcd(unsigned int u, unsigned int v);
+
+/* ---- GB300 additions ---- */
+#define DMG_C128 0 /**< complex128 data, FP64 arithmetic */
+#define DMG_C64 1  /**< complex64 data, FP32 arithmetic */
+
+/** makeSplitPlan for a given element type (DMG_C128 or DMG_C64); `length`
+ * is the per-rank workspace length in elements of that type. */
+SplitPlan dmg_makeSplitPlanTyped(int slab, Decomp start, void *dat, long long length, void *workspace, int dtype);
+/** makeParallelPlan for a given element type. */
+SplitPlan dmg_makeParallelPlanTyped(Decomp start, int *initial_factor, void *dat, long long length,
+                                    void *workspace, int dtype);
+/** Status-returning run on an explicit stream (NULL = legacy default). */
+int dmg_split_run(SplitPlan plan, int direction, void *stream);
+/** Rebind the device buffers of a plan (same sizes). */
+int dmg_split_set_buffers(SplitPlan plan, void *dat, void *workspace);
+/** Per-rank pitch (elements) of the dat array; default extent(start). */
+int dmg_split_set_dat_pitch(SplitPlan plan, long long pitch);
+/** Kernel launches one run makes. */
+int dmg_split_launches(SplitPlan plan, int direction);
+/** 5 N log2 N flops of one 3D transform (the conventional count). */
+double dmg_split_flops(SplitPlan plan);
+/** Turn per-phase CUDA-event timing on or off (off by default). */
+int dmg_split_set_timing(SplitPlan plan, int on);
+/** Synchronise and add the timed phases of past runs into plan->times. */
+int dmg_split_collect_times(SplitPlan plan);
+/** Short description of the pass list. */
+const char *dmg_split_describe(SplitPlan plan);
+
+/** Processor grid over the communicator's ranks for `ndim` task counts
+ * (reference processor_grid.c:73-97); the caller frees the result. */
+int *makeProcessorGrid(MPI_Comm comm, int ndim, int tasks[]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
