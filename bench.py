@@ -1,16 +1,20 @@
 #!/usr/bin/env python3
 """Benchmark of the reshape + split-3D-FFT hot path on one GB300.
 
-Workload (one step): a 512x512x512 complex128 global array on an 8x8 virtual
-processor grid (64 virtual ranks) moves through the decomposition chain
-block -> rotate -> factor_reverse (two reshapes), then the split 3D FFT runs
-forward and inverse on the factor_reverse decomposition.  Inputs are seeded
-uniform[-1,1) values resident in HBM (2 GiB per array, larger than L2, so no
-L2 flush is needed between steps).
+Workload (one step), the plain FP64 drop-in at scale: a 512x512x512
+complex128 global array on an 8x8 virtual processor grid (64 virtual ranks)
+moves through the decomposition chain block -> rotate -> factor_reverse (two
+reshapes), then the split 3D FFT runs forward and inverse on the
+factor_reverse decomposition.  Inputs are seeded uniform[-1,1) values
+resident in HBM (2 GiB per array, larger than the 129 MB L2, so no L2 flush
+is needed between steps).
 
-Prints one JSON line (see the keys below).  ``--impl reference`` times the
-reference algorithm on the host cores instead (the CPU restatement under
-oracle/, since the reference itself needs MPI and FFTW, absent on the box).
+Prints one JSON line.  ``value`` is GFLOP/s of the whole step (two 3D
+transforms at 5 N log2 N flops each, divided by the time of the full step,
+reshapes included); the reshape GB/s and the FFT-only GFLOP/s are reported
+beside it.  ``--impl reference`` times the reference algorithm on the host
+cores instead (the CPU restatement under oracle/: the reference itself needs
+MPI and FFTW, which the GPU machine does not have).
 """
 from __future__ import annotations
 
@@ -30,17 +34,23 @@ sys.path.insert(0, ROOT)
 N_SIDE = 512
 GRID = (8, 8)
 P = GRID[0] * GRID[1]
-ROT = (1, 170)        # rotate amounts on dims 0 and 1 (1 and L/3)
-FREV = ((16, 32), (32, 16))  # factor_reverse (A, B) on dims 0 and 1
 
 
-def specs(n=N_SIDE, grid=GRID, rot=ROT, frev=FREV):
+def specs(n=N_SIDE, grid=GRID):
+    """block -> rotate(1, n/3) -> factor_reverse((16, n/16), (n/16, 16)) on dims 0 and 1; dim 2 local."""
     g0, g1 = grid
+    rot = (1, n // 3)
+    frev = ((16, n // 16), (n // 16, 16))
     blk = "packed:block(%d,%d)|block(%d,%d)|local(%d)" % (n, g0, n, g1, n)
     rotd = "packed:rotate(%d,block(%d,%d))|rotate(%d,block(%d,%d))|local(%d)" % (rot[0], n, g0, rot[1], n, g1, n)
     frv = "packed:frev(%d,%d,block(%d,%d))|frev(%d,%d,block(%d,%d))|local(%d)" % (
         frev[0][0], frev[0][1], n, g0, frev[1][0], frev[1][1], n, g1, n)
     return blk, rotd, frv
+
+
+def workload_name(n):
+    return ("%d^3 complex128, 8x8 virtual grid: reshape block->rotate(1,%d)->factor_reverse((16,%d),(%d,16)), "
+            "split 3D FFT forward + inverse" % (n, n // 3, n // 16, n // 16))
 
 
 def measured_peaks():
@@ -52,12 +62,12 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel_key):
+def ncu_traffic(key):
     """DRAM bytes per launch of a kernel from the committed ncu summary, if any."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(p):
         with open(p) as f:
-            return json.load(f).get(kernel_key)
+            return json.load(f).get(key)
     return None
 
 
@@ -120,21 +130,21 @@ def flops_per_transform(n_total):
 # ----------------------------------------------------------------------------- GPU arm
 
 def run_gpu(args):
-    import numpy as np
     import torch
 
     from decomp_mpi_gb300 import api
 
     dev = torch.device("cuda:0")
     torch.cuda.set_device(dev)
-    blk, rotd, frv = specs()
+    n = args.n
+    blk, rotd, frv = specs(n)
     comm = api.Comm(P)
     D0 = api.decomp_from_spec(comm, blk)
     D1 = api.decomp_from_spec(comm, rotd)
     D2 = api.decomp_from_spec(comm, frv)
     r01 = api.ReshapePlan(comm, 16, D0, D1)
     r12 = api.ReshapePlan(comm, 16, D1, D2)
-    n_total = N_SIDE ** 3
+    n_total = n ** 3
     stream = torch.cuda.current_stream(dev)
     sh = stream.cuda_stream
 
@@ -146,17 +156,26 @@ def run_gpu(args):
     a1 = torch.empty(P * r01.dest_pitch, dtype=torch.complex128, device=dev)
     a2 = torch.empty(P * r12.dest_pitch, dtype=torch.complex128, device=dev)
 
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
-    reshape_ms = []
+    # workspace sized as the reference requires: 2 * extent per rank
+    probe = api.SplitPlan(D2, 1 << 20, 1 << 40, 1 << 21)
+    length = 2 * probe.extent
+    probe.free()
+    work = torch.empty(P * length, dtype=torch.complex128, device=dev)
+    sp = api.SplitPlan(D2, a2.data_ptr(), length, work.data_ptr())
+
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
 
     def step(record=False):
         if record:
             ev[0].record(stream)
         r01.run(a0.data_ptr(), a1.data_ptr(), sh)
+        r12.run(a1.data_ptr(), a2.data_ptr(), sh)
         if record:
             ev[1].record(stream)
+        sp.run(api.FFTW_FORWARD, sh)
+        if record:
             ev[2].record(stream)
-        r12.run(a1.data_ptr(), a2.data_ptr(), sh)
+        sp.run(api.FFTW_BACKWARD, sh)
         if record:
             ev[3].record(stream)
 
@@ -165,7 +184,7 @@ def run_gpu(args):
     torch.cuda.synchronize()
     clocks = ClockSampler()
     clocks.start()
-    time.sleep(0.3)
+    time.sleep(0.4)
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
@@ -175,35 +194,62 @@ def run_gpu(args):
     t1.record(stream)
     torch.cuda.synchronize()
     total_ms = t0.elapsed_time(t1)
-    # per-kernel durations (same stream, separate pass so the headline loop has no extra events)
-    for _ in range(args.steps):
-        step(record=True)
-        torch.cuda.synchronize()
-        reshape_ms.append(ev[0].elapsed_time(ev[1]))
-        reshape_ms.append(ev[2].elapsed_time(ev[3]))
     clk = clocks.stop()
 
-    # correctness spot check of this run: reshape back and compare (bit-exact permutation)
-    r20 = api.ReshapePlan(comm, 16, D2, D0)
-    back = torch.empty_like(a0)
-    r20.run(a2.data_ptr(), back.data_ptr(), sh)
+    # component times (a separate pass with events between the parts)
+    res_ms, fwd_ms, inv_ms = [], [], []
+    for _ in range(max(2, min(args.steps, 5))):
+        step(record=True)
+        torch.cuda.synchronize()
+        res_ms.append(ev[0].elapsed_time(ev[1]))
+        fwd_ms.append(ev[1].elapsed_time(ev[2]))
+        inv_ms.append(ev[2].elapsed_time(ev[3]))
+    # per-pass kernel durations of the dominant kernel (FFT pass), same stream
+    sp.set_timing(True)
+    step()
+    torch.cuda.synchronize()
+    sp.run(api.FFTW_FORWARD, sh)
+    torch.cuda.synchronize()
+    pass_fwd = sp.pass_times(api.FFTW_FORWARD)
+    sp.run(api.FFTW_BACKWARD, sh)
+    torch.cuda.synchronize()
+    pass_inv = sp.pass_times(api.FFTW_BACKWARD)
+    sp.set_timing(False)
+
+    # correctness of this run: forward then inverse returns N times the input
+    r01.run(a0.data_ptr(), a1.data_ptr(), sh)
+    r12.run(a1.data_ptr(), a2.data_ptr(), sh)
+    ref = a2.clone()
+    sp.run(api.FFTW_FORWARD, sh)
+    sp.run(api.FFTW_BACKWARD, sh)
     torch.cuda.synchronize()
     from oracle import oracle as O  # the checker only
-    off = torch.from_numpy(O.global_offsets(P, blk, r01.src_pitch, (N_SIDE,) * 3).ravel()).to(dev)
-    exact = bool(torch.equal(back[off], a0[off]))
+    off = torch.from_numpy(O.global_offsets(P, frv, r12.dest_pitch, (n,) * 3).ravel()).to(dev)
+    back = a2[off] / n_total
+    want = ref[off]
+    rt_err = float((torch.linalg.vector_norm(back - want) / torch.linalg.vector_norm(want)).item())
+    del off, back, want, ref
 
     ms_per_step = total_ms / args.steps
-    bytes_step = r01.bytes_moved + r12.bytes_moved
-    gbs = bytes_step / (ms_per_step * 1e-3) / 1e9
+    flops_step = 2 * flops_per_transform(n_total)
+    gflops = flops_step / (ms_per_step * 1e-3) / 1e9
+    reshape_bytes = r01.bytes_moved + r12.bytes_moved
+    reshape_gbs = reshape_bytes / (statistics.median(res_ms) * 1e-3) / 1e9
+    fft_ms = statistics.median(fwd_ms) + statistics.median(inv_ms)
+    fft_gflops = flops_step / (fft_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
-    per_launch_ms = statistics.mean(reshape_ms)
-    achieved = r01.bytes_moved / (per_launch_ms * 1e-3) / 1e9
+    launches = pass_fwd + pass_inv
+    avg_pass_ms = statistics.mean(launches)
+    pass_bytes = 2.0 * n_total * 16  # algorithmic bytes of one pass: read + write the array once
+    achieved = pass_bytes / (avg_pass_ms * 1e-3) / 1e9
+    fp64_peak = api.load().dmg_probe_fma_tflops(0)
+    pass_tflops = flops_per_transform(n_total) / len(pass_fwd) / (avg_pass_ms * 1e-3) / 1e12
 
-    # end to end through the C-ABI with host buffers: H2D input, two reshapes, D2H result
+    # end to end through the C-ABI with host buffers: H2D input, the step, D2H result
     host_in = torch.empty(a0.numel(), dtype=torch.complex128, pin_memory=True)
     host_in.copy_(a0.cpu())
     host_out = torch.empty(a2.numel(), dtype=torch.complex128, pin_memory=True)
-    for _ in range(max(1, args.warmup // 2)):
+    for _ in range(2):
         a0.copy_(host_in, non_blocking=True)
         step()
         host_out.copy_(a2, non_blocking=True)
@@ -218,88 +264,105 @@ def run_gpu(args):
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1) / args.steps
-    e2e = {"value": round(bytes_step / (e2e_ms * 1e-3) / 1e9, 2), "unit": "GB/s",
+    e2e = {"value": round(flops_step / (e2e_ms * 1e-3) / 1e9, 2), "unit": "GFLOP/s",
            "h2d_bytes_per_step": host_in.numel() * 16, "d2h_bytes_per_step": host_out.numel() * 16,
-           "ms_per_step": round(e2e_ms, 4)}
+           "ms_per_step": round(e2e_ms, 3)}
 
-    cpu = cpu_baseline(args, sample_only=True)
+    cpu = cpu_baseline(args, reps=1)
     line = {
-        "metric": "reshape GB/s (block->rotate->factor_reverse chain, 512^3 complex128, 8x8 virtual grid)",
-        "value": round(gbs, 2),
-        "unit": "GB/s",
+        "metric": "3D FFT GFLOP/s (5 N log2 N per transform) + reshape GB/s",
+        "value": round(gflops, 2),
+        "unit": "GFLOP/s",
         "n_gpus": 1,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": round(ms_per_step, 4),
+        "ms_per_step": round(ms_per_step, 3),
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "c128",
+        "dtype": "f64",
         "data": "synthetic: uniform[-1,1) complex128, seed 1, resident in HBM",
-        "config": {"workload": "512^3 complex128, 8x8 virtual grid, reshape block->rotate(1,170)->"
-                               "factor_reverse((16,32),(32,16))", "virtual_ranks": P,
-                   "l2": "inputs (2 GiB) larger than L2, no flush", "parallelism": "virtual grid on one GPU"},
-        "bit_exact_roundtrip": exact,
+        "config": {"workload": workload_name(n), "virtual_ranks": P, "dat_pitch": r12.dest_pitch,
+                   "work_length_per_rank": length, "l2": "inputs (2 GiB) larger than L2, no flush",
+                   "parallelism": "8x8 virtual grid on one GPU"},
+        "fft_gflops": round(fft_gflops, 2),
+        "reshape_gbs": round(reshape_gbs, 1),
+        "reshape_frac_of_hbm": round(reshape_gbs / peak, 4),
+        "ms_breakdown": {"reshapes": round(statistics.median(res_ms), 3),
+                         "fft_forward": round(statistics.median(fwd_ms), 3),
+                         "fft_inverse": round(statistics.median(inv_ms), 3)},
+        "fft_pass_ms": [round(x, 3) for x in launches],
+        "roundtrip_rel_l2": rt_err,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                     "traffic": ncu_traffic("reshape_512c128_block_to_rotate"),
-                     "kernel": "k1_permute (block->rotate reshape), algorithmic bytes 2*N*16"},
+                     "traffic": ncu_traffic("fft_pass_512c128"),
+                     "kernel": "fft_pass_kernel<double> (one split-FFT pass: 2*N*16 B algorithmic)",
+                     "fp64": {"achieved_tflops": round(pass_tflops, 3), "peak_tflops": round(fp64_peak, 3),
+                              "frac": round(pass_tflops / fp64_peak, 4) if fp64_peak > 0 else None,
+                              "note": "5 N log2(n) flops per pass; peak from the in-library FMA probe"}},
         "e2e": e2e,
-        "gpu_launches": (r01.launches + r12.launches) * args.steps,
+        "gpu_launches": (r01.launches + r12.launches + sp.launches(api.FFTW_FORWARD)
+                         + sp.launches(api.FFTW_BACKWARD)) * args.steps,
         "clocks": clk,
         "cpu_baseline": cpu,
-        "plans": [r01.describe(), r12.describe()],
+        "plans": {"reshape": [r01.describe(), r12.describe()], "split": sp.describe()},
     }
     print(json.dumps(line))
 
 
 # ----------------------------------------------------------------------------- CPU arm (reference algorithm)
 
-def cpu_baseline(args, sample_only=False):
-    """The reference's reshape algorithm (oracle restatement: per-peer typemaps, pack and unpack)
-    on the host cores, over a bounded sample: the same chain at 256^3 on the same 8x8 grid."""
+def cpu_baseline(args, reps=1, n=256):
+    """The reference's algorithm on the host cores over a bounded sample of the workload: the same
+    chain and split FFT at n^3 on the same 8x8 grid, restated in C (per-peer typemaps packed and
+    unpacked for the reshapes; FFT stages on the oracle's FP64 FFT, standing in for FFTW)."""
     import numpy as np
 
     from oracle import oracle as O
 
-    n = 256
-    blk, rotd, frv = specs(n=n, rot=(1, 85), frev=((16, 16), (32, 8)))
+    blk, rotd, frv = specs(n)
     threads = os.cpu_count() or 1
-    sp, p1, p2 = O.pitch_of(P, blk), O.pitch_of(P, rotd), O.pitch_of(P, frv)
+    sp0, p1, p2 = O.pitch_of(P, blk), O.pitch_of(P, rotd), O.pitch_of(P, frv)
     rng = np.random.default_rng(1)
-    a0 = rng.uniform(-1, 1, P * sp) + 1j * rng.uniform(-1, 1, P * sp)
+    a0 = rng.uniform(-1, 1, P * sp0) + 1j * rng.uniform(-1, 1, P * sp0)
     a1 = np.zeros(P * p1, np.complex128)
     a2 = np.zeros(P * p2, np.complex128)
     pl1 = O.ReshapePlanCPU(P, blk, rotd, 16)
     pl2 = O.ReshapePlanCPU(P, rotd, frv, 16)
-    pl1.run(a0, sp, a1, p1, threads)
-    reps = 2 if sample_only else max(1, args.steps)
+    wl = 4 * (n ** 3) // P + 64  # at least twice the extent of A and B on every rank
+    fft = O.SplitPlanCPU(P, frv, wl)
+    work = np.zeros(P * wl, np.complex128)
+
+    def one():
+        pl1.run(a0, sp0, a1, p1, threads)
+        pl2.run(a1, p1, a2, p2, threads)
+        fft.run(a2, p2, work, -1, threads)
+        fft.run(a2, p2, work, +1, threads)
+
     t = time.perf_counter()
     for _ in range(reps):
-        pl1.run(a0, sp, a1, p1, threads)
-        pl2.run(a1, p1, a2, p2, threads)
+        one()
     dt = (time.perf_counter() - t) / reps
-    gbs = 2 * 2 * (n ** 3) * 16 / dt / 1e9
-    return {"value": round(gbs, 3), "unit": "GB/s", "cores": threads, "kind": "port",
-            "sample": "reshape chain block->rotate->factor_reverse at 256^3 complex128 on the 8x8 virtual grid, "
-                      "reference algorithm restated in C (per-peer typemaps, pack + unpack), %d threads" % threads,
+    flops = 2 * flops_per_transform(n ** 3)
+    return {"value": round(flops / dt / 1e9, 3), "unit": "GFLOP/s", "cores": threads, "kind": "port",
+            "sample": "the same step at %d^3 complex128 on the 8x8 virtual grid (64 ranks on %d threads): "
+                      "reshape chain with the reference's per-peer typemaps (pack + unpack) and the split FFT "
+                      "with the oracle's FP64 FFT in place of FFTW" % (n, threads),
             "ms_per_step": round(dt * 1e3, 2)}
 
 
 def run_reference(args):
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
+    if int(os.environ.get("RANK", "0")) != 0:
         return
-    cpu = cpu_baseline(args)
+    cpu = cpu_baseline(args, reps=max(1, min(args.steps, 5)))
     line = {
-        "metric": "reshape GB/s (block->rotate->factor_reverse chain, 512^3 complex128, 8x8 virtual grid)",
-        "value": cpu["value"], "unit": "GB/s", "n_gpus": int(args.gpus), "steps": args.steps,
+        "metric": "3D FFT GFLOP/s (5 N log2 N per transform) + reshape GB/s",
+        "value": cpu["value"], "unit": "GFLOP/s", "n_gpus": int(args.gpus), "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": cpu["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "c128", "data": "synthetic: uniform[-1,1) complex128, seed 1",
-        "config": {"workload": "512^3 complex128, 8x8 virtual grid, reshape block->rotate->factor_reverse "
-                               "(bounded CPU sample at 256^3)", "virtual_ranks": P},
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic: uniform[-1,1) complex128, seed 1",
+        "config": {"workload": workload_name(args.n) + " (bounded CPU sample at 256^3)", "virtual_ranks": P},
         "impl": "reference", "cpu_baseline": cpu,
-        "e2e": {"value": cpu["value"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "e2e": {"value": cpu["value"], "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
 
@@ -310,9 +373,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=N_SIDE, help="cube side (the headline workload is 512)")
     args = ap.parse_args()
-    if args.warmup < 3:
-        args.warmup = 3
+    args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         run_reference(args)
         return

@@ -102,6 +102,8 @@ SIGNATURES = {
     "dmg_split_describe": (_cp, [_vp]),
     "dmg_split_set_timing": (_i, [_vp, _i]),
     "dmg_split_collect_times": (_i, [_vp]),
+    "dmg_split_pass_times": (_i, [_vp, _i, ctypes.POINTER(ctypes.c_float), _i]),
+    "dmg_probe_fma_tflops": (ctypes.c_double, [_i]),
 }
 
 _lib = None

@@ -403,6 +403,23 @@ class SplitPlan:
     def run(self, direction=FFTW_FORWARD, stream=None):
         check(self.lib.dmg_split_run(self.h, int(direction), ctypes.c_void_p(stream or 0)), "runSplitPlan")
 
+    def set_timing(self, on=True):
+        check(self.lib.dmg_split_set_timing(self.h, int(bool(on))), "dmg_split_set_timing")
+
+    def pass_times(self, direction=FFTW_FORWARD):
+        """Milliseconds of each pass of the last timed run in `direction`."""
+        buf = (ctypes.c_float * 16)()
+        k = self.lib.dmg_split_pass_times(self.h, int(direction), buf, 16)
+        if k < 0:
+            raise DecompError("dmg_split_pass_times: %s" % last_error())
+        return [buf[i] for i in range(k)]
+
+    def times(self):
+        """plan->times after dmg_split_collect_times: {name: seconds}."""
+        check(self.lib.dmg_split_collect_times(self.h), "dmg_split_collect_times")
+        t = self._s.times
+        return {n: t[i] for i, n in enumerate(["RESHAPE_1", "FFT_1", "TWIDDLE", "RESHAPE_2", "FFT_2", "ALL"])}
+
     def launches(self, direction=FFTW_FORWARD):
         return self.lib.dmg_split_launches(self.h, int(direction))
 

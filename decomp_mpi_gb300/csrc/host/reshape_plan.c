@@ -390,6 +390,8 @@ static void choose_tiles(struct dmg_k1_params *kp, const int *len, int na, int a
     if (e1max > 64) e1max = 64;
     kp->e1 = len[ax_d] < e1max ? len[ax_d] : e1max;
   } else {
+    /* same fast axis: the direct kernel moves 2048 units per tile without shared memory */
+    tile_units = 2048;
     kp->ax0 = ax_s;
     kp->load_fast = 0;
     kp->store_fast = 0;

@@ -80,6 +80,7 @@ struct dmg_split_impl {
   void *dat, *work;
   int timing;
   void *events;
+  int timed_dir, timed_passes, collected;
   char desc[768];
 };
 
@@ -375,10 +376,11 @@ static int impl_upload(struct dmg_split_impl *im) {
   int nd = im->ndim;
   size_t cs = im->dtype == DMG_C128 ? 16 : 8;
   size_t bytes = 0;
+  fft_layout *all[3] = {&im->lay[0], &im->lay[1], &im->lay[2]};
   for (int k = 0; k < 3; ++k) {
-    if (!im->lay[k].tab[0]) continue;
+    if (!all[k]->tab[0]) continue;
     for (int d = 0; d < nd; ++d) bytes += align256((size_t)im->L[d] * 8) + align256((size_t)im->L[d] * 4);
-    if (im->lay[k].ranked) bytes += align256((size_t)nd * im->lay[k].nranks * 8);
+    if (all[k]->ranked) bytes += align256((size_t)nd * all[k]->nranks * 8);
   }
   for (int k = 0; k < im->nfwd; ++k) bytes += align256((size_t)im->fwd[k].p.n * cs);
   for (int d = 0; d < nd; ++d) bytes += align256((size_t)im->L[d] * cs);
@@ -391,7 +393,7 @@ static int impl_upload(struct dmg_split_impl *im) {
   }
   size_t pos = 0;
   for (int k = 0; k < 3; ++k) {
-    fft_layout *l = &im->lay[k];
+    fft_layout *l = all[k];
     if (!l->tab[0]) continue;
     for (int d = 0; d < nd; ++d) {
       memcpy(host + pos, l->tab[d], (size_t)im->L[d] * 8);
@@ -795,15 +797,42 @@ const char *dmg_split_describe(SplitPlan plan) { return plan ? plan->impl->desc 
 int dmg_split_set_timing(SplitPlan plan, int on) {
   if (!plan) return dmg_error(DMG_ERR_ARG, "NULL plan");
   plan->impl->timing = on;
-  if (on && !plan->impl->events) plan->impl->events = dmg_split_create_events(2 * (MAXPASS + 2));
+  if (on && !plan->impl->events) plan->impl->events = dmg_split_create_events(MAXPASS + 1);
   return DMG_OK;
+}
+
+/* Event k precedes pass k of the last timed run, event K follows the last. */
+int dmg_split_pass_times(SplitPlan plan, int direction, float *ms, int max) {
+  if (!plan) return dmg_error(DMG_ERR_ARG, "NULL plan");
+  struct dmg_split_impl *im = plan->impl;
+  if (!im->events || im->timed_dir != direction) return dmg_error(DMG_ERR_ARG, "no timed run in that direction");
+  int K = im->timed_passes;
+  for (int k = 0; k < K && k < max; ++k) {
+    int st = dmg_split_event_elapsed(im->events, k, k + 1, &ms[k]);
+    if (st != DMG_OK) return st;
+  }
+  return K;
 }
 
 int dmg_split_collect_times(SplitPlan plan) {
   if (!plan) return dmg_error(DMG_ERR_ARG, "NULL plan");
   struct dmg_split_impl *im = plan->impl;
-  if (!im->events) return DMG_OK;
-  (void)im;
+  if (!im->events || im->timed_passes <= 0 || im->collected) return DMG_OK;
+  float ms[MAXPASS];
+  int K = dmg_split_pass_times(plan, im->timed_dir, ms, MAXPASS);
+  if (K < 0) return K;
+  /* stage-1 passes count as FFT_1 (with the fused start->A move and the
+   * twiddle), stage-2 passes as FFT_2 (with the fused A->B move) */
+  pass_rec *list = im->timed_dir == FFTW_FORWARD ? im->fwd : im->inv;
+  double all = 0;
+  for (int k = 0; k < K; ++k) {
+    double sec = ms[k] * 1e-3;
+    all += sec;
+    if (list[k].p.t & 1) plan->times[FFT_1] += sec;
+    else plan->times[FFT_2] += sec;
+  }
+  plan->times[ALL] += all;
+  im->collected = 1;
   return DMG_OK;
 }
 
@@ -825,12 +854,20 @@ int dmg_split_run(SplitPlan plan, int direction, void *stream) {
   pass_rec *list = direction == FFTW_FORWARD ? im->fwd : im->inv;
   int cnt = direction == FFTW_FORWARD ? im->nfwd : im->ninv;
   int dt = im->dtype == DMG_C128 ? 0 : 1;
+  if (im->timing) {
+    if (im->timed_passes > 0 && !im->collected) dmg_split_collect_times(plan);
+    im->timed_dir = direction;
+    im->timed_passes = cnt;
+    im->collected = 0;
+  }
   for (int k = 0; k < cnt; ++k) {
     const void *src = list[k].in_buf == BUF_DAT ? im->dat : im->work;
     void *dst = list[k].out_buf == BUF_DAT ? im->dat : im->work;
+    if (im->timing) dmg_split_record_event(im->events, k, stream);
     int st = dmg_fft_pass_launch(&list[k].p, dt, src, dst, stream);
     if (st != DMG_OK) return st;
   }
+  if (im->timing) dmg_split_record_event(im->events, cnt, stream);
   return DMG_OK;
 }
 

@@ -22,7 +22,7 @@
 namespace {
 
 constexpr int NT = 256;
-constexpr int TILE_MAX = 2048;  // complex values per tile buffer
+constexpr int TILE_MAX = 4096;  // complex values per tile buffer (one 4096-long line at most)
 
 template <typename T>
 using C2 = typename std::conditional<std::is_same<T, double>::value, double2, float2>::type;

@@ -209,8 +209,123 @@ __global__ void __launch_bounds__(NT) k1_permute(const dmg_k1_params p, const U 
   }
 }
 
+// Address of (i0, i1) of a tile from global tables (direct kernel).
+template <bool RANKED>
+__device__ __forceinline__ int64_t direct_addr(const dmg_k1_side &s, int64_t base, int32_t rbase, const int64_t *bto,
+                                               const int32_t *bax, int nbatch, int ax0, int ax1, int g0, int g1) {
+  if constexpr (!RANKED) {
+    int64_t a = base + __ldg(s.tab[ax0] + g0);
+    if (ax1 >= 0) a += __ldg(s.tab[ax1] + g1);
+    return a;
+  } else {
+    int32_t R = rbase + __ldg(s.rk[ax0] + g0);
+    if (ax1 >= 0) R += __ldg(s.rk[ax1] + g1);
+    if (R < 0) return -1;
+    const int64_t *rs = s.rstride;
+    const int P = s.nranks;
+    int64_t a = (int64_t)R * s.pitch + __ldg(s.tab[ax0] + g0) * __ldg(rs + (size_t)ax0 * P + R);
+    if (ax1 >= 0) a += __ldg(s.tab[ax1] + g1) * __ldg(rs + (size_t)ax1 * P + R);
+    for (int b = 0; b < nbatch; ++b) a += bto[b] * __ldg(rs + (size_t)bax[b] * P + R);
+    return a;
+  }
+}
+
+// Same fast axis on both sides: every thread moves its own elements straight
+// from source to destination, MAXITEMS loads in flight before the stores,
+// with no shared memory and no barrier.  Tiles run along ax0 (contiguous on
+// both sides) and ax1.
+template <typename U, bool SR, bool DR>
+__global__ void __launch_bounds__(NT, 4) k1_direct(const dmg_k1_params p, const U *__restrict__ src, U *__restrict__ dst) {
+  const int ax0 = p.ax0, ax1 = p.ax1;
+  const int e0 = p.e0, e1 = p.e1;
+  const int tid = threadIdx.x;
+  for (int64_t tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
+    int64_t t = tile;
+    const int t0 = (int)(t % p.nt0);
+    t /= p.nt0;
+    int t1 = 0;
+    if (ax1 >= 0) {
+      t1 = (int)(t % p.nt1);
+      t /= p.nt1;
+    }
+    int64_t sb = 0, db = 0;
+    int32_t rs = 0, rd = 0;
+    int64_t sbto[DMG_MAXAX], dbto[DMG_MAXAX];
+    int32_t bax[DMG_MAXAX];
+#pragma unroll
+    for (int b = 0; b < DMG_MAXAX; ++b) {
+      if (b < p.nbatch) {
+        const int a = p.batch_ax[b];
+        const int c = (int)(t % p.len[a]);
+        t /= p.len[a];
+        bax[b] = a;
+        if constexpr (SR) {
+          rs += __ldg(p.src.rk[a] + c);
+          sbto[b] = __ldg(p.src.tab[a] + c);
+        } else {
+          sb += __ldg(p.src.tab[a] + c);
+        }
+        if constexpr (DR) {
+          rd += __ldg(p.dst.rk[a] + c);
+          dbto[b] = __ldg(p.dst.tab[a] + c);
+        } else {
+          db += __ldg(p.dst.tab[a] + c);
+        }
+      }
+    }
+    if ((SR ? rs < 0 : sb < 0) || (DR ? rd < 0 : db < 0)) continue;
+    const int g0 = t0 * e0, g1 = t1 * e1;
+    const int lim0 = min(e0, p.len[ax0] - g0);
+    const int lim1 = ax1 >= 0 ? min(e1, p.len[ax1] - g1) : 1;
+    const int n = lim0 * lim1;
+    int q = tid / lim0, r = tid - q * lim0;
+    const int dq = NT / lim0, dr = NT - (NT / lim0) * lim0;
+    U v[MAXITEMS];
+    int64_t da[MAXITEMS];
+#pragma unroll
+    for (int j = 0; j < MAXITEMS; ++j) {
+      da[j] = -1;
+      if (tid + j * NT < n) {
+        int64_t d = direct_addr<DR>(p.dst, db, rd, dbto, bax, p.nbatch, ax0, ax1, g0 + r, g1 + q);
+        int64_t s = direct_addr<SR>(p.src, sb, rs, sbto, bax, p.nbatch, ax0, ax1, g0 + r, g1 + q);
+        if (d >= 0 && s >= 0) {
+          v[j] = src[s];
+          da[j] = d;
+        }
+      }
+      r += dr;
+      q += dq;
+      if (r >= lim0) {
+        r -= lim0;
+        q += 1;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < MAXITEMS; ++j)
+      if (da[j] >= 0) dst[da[j]] = v[j];
+  }
+}
+
+template <typename U, bool SR, bool DR>
+int launch_direct(const dmg_k1_params &p, const void *src, void *dst, cudaStream_t stream) {
+  auto kern = k1_direct<U, SR, DR>;
+  int dev = 0, nsm = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, 0);
+  if (per_sm < 1) per_sm = 1;
+  int64_t grid = (int64_t)nsm * per_sm;
+  if (grid > p.ntiles) grid = p.ntiles;
+  if (grid < 1) return DMG_OK;
+  kern<<<(unsigned)grid, NT, 0, stream>>>(p, static_cast<const U *>(src), static_cast<U *>(dst));
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return dmg_error(DMG_ERR_CUDA, "reshape kernel launch: %s", cudaGetErrorString(e));
+  return DMG_OK;
+}
+
 template <typename U, bool SR, bool DR>
 int launch_typed(const dmg_k1_params &p, const void *src, void *dst, cudaStream_t stream) {
+  if (p.load_fast == p.store_fast) return launch_direct<U, SR, DR>(p, src, dst, stream);
   const size_t tilebytes = (sizeof(U) * (size_t)p.e1 * (p.e0 + 1) + 15) & ~size_t(15);
   const size_t smem = tilebytes + (size_t)(p.e0 + p.e1) * 2 * (sizeof(int64_t) + sizeof(int32_t));
   auto kern = k1_permute<U, SR, DR>;

@@ -142,8 +142,13 @@ int dmg_split_launches(SplitPlan plan, int direction);
 double dmg_split_flops(SplitPlan plan);
 /** Turn per-phase CUDA-event timing on or off (off by default). */
 int dmg_split_set_timing(SplitPlan plan, int on);
-/** Synchronise and add the timed phases of past runs into plan->times. */
+/** Synchronise and add the timed passes of the last timed run into
+ * plan->times (FFT_1: stage-1 passes with the fused start->A move and
+ * twiddle; FFT_2: stage-2 passes with the fused A->B move; ALL). */
 int dmg_split_collect_times(SplitPlan plan);
+/** Per-pass milliseconds of the last timed run in `direction` (timing on);
+ * returns the number of passes or a negative error. */
+int dmg_split_pass_times(SplitPlan plan, int direction, float *ms, int max);
 /** Short description of the pass list. */
 const char *dmg_split_describe(SplitPlan plan);
 

@@ -70,6 +70,14 @@ CASES = [
     ("struct48_3d", 4, "packed:block(8,2)|block(6,2)|local(5)", "packed:local(8)|local(6)|block(5,4)", "V48"),
     ("four_dims", 8, "packed:block(6,2)|block(4,2)|block(6,2)|local(10)",
      "packed:local(6)|rotate(1,block(4,4))|local(6)|block(10,2)", "complex64"),
+    # explicit strides whose fast axes differ: the shared-memory transpose kernel
+    ("transpose_2d", 4, "axes:block(64,2)@1,1|block(48,2)@32,2", "axes:block(64,2)@24,1|block(48,2)@1,2",
+     "complex128"),
+    ("transpose_3d_int64", 8, "axes:block(40,2)@1,1|block(36,2)@20,2|block(10,2)@360,4",
+     "axes:local(40)@180,1|block(36,4)@1,2|block(10,2)@9,1", "int64"),
+    ("transpose_uneven_ranked", 6, "packed:block(10,3)|block(7,2)|local(9)",
+     "axes:local(10)@9,1|block(7,3)@1,1|block(9,2)@30,3", "float32"),
+    ("transpose_int8", 4, "axes:block(33,2)@1,1|block(20,2)@17,2", "axes:block(33,2)@10,1|block(20,2)@1,2", "int8"),
     # explicit strides with padding, single-rank source (test.c pattern)
     ("single_source_3d", 4, "axes:single(12,0,1)@1,1|single(10,0,4)@12,1|local(6)@130,1",
      "axes:rotate(2,local(12))@1,1|rotate(1,block(10,4))@12,1|local(6)@40,1", "float64"),

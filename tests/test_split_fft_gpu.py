@@ -1,0 +1,139 @@
+"""GPU split 3D FFT through the C-ABI against the reference's fixtures and the FP64 oracle."""
+import numpy as np
+import pytest
+
+from decomp_mpi_gb300 import api
+from oracle import oracle as O
+from tests.golden_cases import split_case, split_names
+
+pytestmark = pytest.mark.gpu
+
+TOL_C128 = 1e-12  # relative L2, FP64
+TOL_C64 = 2e-6    # relative L2, FP32
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+class Run:
+    """One split plan on the GPU with its buffers."""
+
+    def __init__(self, P, spec, shape, cuda, mode=0, B=None, dtype=api.C128, work_len=None, seed=0):
+        import torch
+        self.torch = torch
+        self.P, self.spec, self.shape = P, spec, tuple(shape)
+        self.comm = api.Comm(P)
+        self.S = api.decomp_from_spec(self.comm, spec)
+        self.dp = self.S.extent()
+        self.wl = work_len or 2 * int(np.prod(shape))
+        rng = np.random.default_rng(seed)
+        self.glob = rng.uniform(-1, 1, self.shape) + 1j * rng.uniform(-1, 1, self.shape)
+        tdt = torch.complex128 if dtype == api.C128 else torch.complex64
+        self.npdt = np.complex128 if dtype == api.C128 else np.complex64
+        host = O.scatter_global(P, spec, self.glob, self.dp).astype(self.npdt)
+        self.dat = torch.from_numpy(host).to(cuda)
+        self.work = torch.zeros(P * self.wl, dtype=tdt, device=cuda)
+        self.plan = api.SplitPlan(self.S, self.dat.data_ptr(), self.wl, self.work.data_ptr(),
+                                  slab=mode if mode < 2 else 0, B=B if mode == 2 else None, dtype=dtype)
+        self.mode, self.B = mode, B
+        self.stream = torch.cuda.current_stream(cuda).cuda_stream
+
+    def forward(self):
+        self.plan.run(api.FFTW_FORWARD, self.stream)
+        self.torch.cuda.synchronize()
+        return self.work.cpu().numpy()
+
+    def inverse(self):
+        self.plan.run(api.FFTW_BACKWARD, self.stream)
+        self.torch.cuda.synchronize()
+        return self.dat.cpu().numpy()
+
+
+@pytest.mark.parametrize("name", split_names())
+def test_golden_forward(name, cuda):
+    """Storage-order parity with the reference's work buffer (FFTW replaced by the FP64 oracle FFT)."""
+    import torch
+    m, z = split_case(name)
+    P, wl = m["P"], m["work_len"]
+    comm = api.Comm(P)
+    S = api.decomp_from_spec(comm, m["spec"])
+    assert S.extent() == m["dat_pitch"]
+    dat = torch.from_numpy(z["dat"].copy()).to(cuda)
+    work = torch.zeros(P * wl, dtype=torch.complex128, device=cuda)
+    plan = api.SplitPlan(S, dat.data_ptr(), wl, work.data_ptr(), slab=m["mode"] if m["mode"] < 2 else 0,
+                         B=m["B"] if m["mode"] == 2 else None)
+    plan.run(api.FFTW_FORWARD, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    got = work.cpu().numpy()
+    held = z["slot"] >= 0
+    assert _rel(got[held], z["work"][held]) < TOL_C128
+
+
+CASES = [
+    # (P, start spec, shape, mode, B)
+    (4, "packed:block(64,2)|block(64,2)|local(64)", (64, 64, 64), 0, None),  # config: 64^3 on 2x2
+    (4, "packed:local(8)|block(12,2)|block(16,2)", (8, 12, 16), 0, None),
+    (16, "packed:block(48,4)|rotate(5,block(48,4))|local(48)", (48, 48, 48), 0, None),
+    (16, "packed:block(120,4)|block(120,4)|local(120)", (120, 120, 120), 0, None),
+    (8, "packed:block(14,2)|block(21,4)|local(11)", (14, 21, 11), 0, None),  # primes 7, 11, 3
+    (4, "packed:local(8)|block(12,2)|block(16,2)", (8, 12, 16), 1, None),     # slab
+    (4, "packed:local(8)|block(12,2)|block(16,2)", (8, 12, 16), 2, [8, 12, 16]),  # every A = 1
+    (4, "packed:local(8)|block(12,2)|block(16,2)", (8, 12, 16), 2, [1, 12, 16]),
+    (4, "packed:block(30,4)", (30,), 0, None),                                 # 1D
+    (4, "packed:block(12,2)|block(18,2)", (12, 18), 0, None),                  # 2D
+    (64, "packed:frev(16,8,block(128,8))|rotate(3,block(64,8))|local(32)", (128, 64, 32), 0, None),
+]
+
+
+@pytest.mark.parametrize("P,spec,shape,mode,B", CASES, ids=[str(c[2]) + "m%d" % c[3] for c in CASES])
+def test_forward_and_inverse_fp64(P, spec, shape, mode, B, cuda):
+    r = Run(P, spec, shape, cuda, mode, B)
+    got = r.forward()
+    exp, mask = O.split_expected_output(P, spec, r.glob, r.wl, mode, B)
+    assert _rel(got[mask], exp[mask]) < TOL_C128
+    back = r.inverse()
+    g = O.gather_global(P, spec, back, r.dp, r.shape) / np.prod(r.shape)
+    assert _rel(g, r.glob) < TOL_C128
+
+
+@pytest.mark.parametrize("P,spec,shape", [
+    (4, "packed:block(64,2)|block(64,2)|local(64)", (64, 64, 64)),
+    (16, "packed:block(120,4)|block(120,4)|local(120)", (120, 120, 120)),
+])
+def test_forward_and_inverse_fp32(P, spec, shape, cuda):
+    r = Run(P, spec, shape, cuda, dtype=api.C64)
+    got = r.forward()
+    exp, mask = O.split_expected_output(P, spec, r.glob, r.wl)
+    assert _rel(got[mask].astype(np.complex128), exp[mask]) < TOL_C64
+    back = r.inverse()
+    g = O.gather_global(P, spec, back.astype(np.complex128), r.dp, r.shape) / np.prod(r.shape)
+    assert _rel(g, r.glob) < TOL_C64
+
+
+def test_delta_input_known_answer(cuda):
+    """fftw_bench.c's delta at the origin: the forward transform is all ones (fftw_bench.c:118-124)."""
+    import torch
+    P, spec, shape = 4, "packed:block(16,2)|block(16,2)|local(16)", (16, 16, 16)
+    r = Run(P, spec, shape, cuda)
+    off = O.global_offsets(P, spec, r.dp, shape)
+    host = np.zeros(P * r.dp, np.complex128)
+    host[off[0, 0, 0]] = 1.0
+    r.dat.copy_(torch.from_numpy(host))
+    got = r.forward()
+    _, mask = O.split_expected_output(P, spec, np.zeros(shape), r.wl)
+    assert np.array_equal(got[mask], np.ones(mask.sum(), np.complex128))
+
+
+def test_linear_index_pattern_roundtrip(cuda):
+    """split_plan_test.c's pattern value = i + L*(j + L*k), forward then backward, scaled by 1/N^3."""
+    import torch
+    P, L = 4, 32
+    spec = "packed:block(%d,2)|block(%d,2)|local(%d)" % (L, L, L)
+    r = Run(P, spec, (L, L, L), cuda)
+    glob = np.arange(L ** 3, dtype=np.float64).reshape(L, L, L) + 0j
+    r.dat.copy_(torch.from_numpy(O.scatter_global(P, spec, glob, r.dp)))
+    r.forward()
+    back = r.inverse()
+    g = O.gather_global(P, spec, back, r.dp, (L, L, L)) / L ** 3
+    assert np.max(np.abs(g - glob)) < 1e-9

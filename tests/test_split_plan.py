@@ -1,0 +1,114 @@
+"""Split-FFT planning on the host against the oracle and the reference's fixtures (no GPU)."""
+import numpy as np
+import pytest
+
+from decomp_mpi_gb300 import api
+from oracle import oracle as O
+from tests.golden_cases import meta, split_case, split_names
+
+PLAN_CASES = [
+    (4, "packed:local(8)|block(12,2)|block(16,2)", 0, None),
+    (4, "packed:block(16,2)|block(16,2)|local(16)", 0, None),
+    (6, "packed:block(12,3)|block(10,2)|local(6)", 0, None),
+    (4, "packed:local(8)|block(12,2)|block(16,2)", 1, None),
+    (4, "packed:local(8)|block(12,2)|block(16,2)", 2, [1, 12, 16]),
+    (64, "packed:block(512,8)|block(512,8)|local(512)", 0, None),
+    (16, "packed:block(120,4)|block(120,4)|local(120)", 0, None),
+    (16, "packed:block(48,4)|rotate(5,block(48,4))|local(48)", 0, None),
+    (4, "packed:block(64,2)|block(64,2)|local(64)", 0, None),
+    (8, "packed:block(14,2)|block(21,4)|local(11)", 0, None),
+    (4, "packed:block(30,4)", 0, None),
+    (4, "packed:block(12,2)|block(18,2)", 0, None),
+]
+
+
+def _work_len(shape):
+    return 2 * int(np.prod(shape))
+
+
+def _shape(P, spec):
+    c = api.Comm(P)
+    return c, api.decomp_from_spec(c, spec)
+
+
+@pytest.mark.parametrize("P,spec,mode,B", PLAN_CASES)
+def test_factors_grids_and_layout_match_oracle(P, spec, mode, B):
+    c, S = _shape(P, spec)
+    lib = S.lib
+    sizes = []
+    import ctypes
+
+    class DS(ctypes.Structure):
+        _fields_ = [("ndim", ctypes.c_int), ("comm", ctypes.c_void_p), ("proc_used", ctypes.c_int),
+                    ("dims", ctypes.POINTER(ctypes.c_void_p))]
+
+    class AD(ctypes.Structure):
+        _fields_ = [("decomp", ctypes.c_void_p)]
+    ds = DS.from_address(S.h)
+    for i in range(ds.ndim):
+        sizes.append(lib.sizeDimDecomp(AD.from_address(ds.dims[i]).decomp))
+    wl = _work_len(sizes)
+    sp = api.SplitPlan(S, 0x100000, wl, 0x200000, slab=mode if mode < 2 else 0, B=B if mode == 2 else None)
+    A, Bf, ga, gb, a_spec, b_spec = O.split_factors(P, spec, mode, B)
+    assert sp.A_factors == A
+    use_first = all(a == 1 for a in A)
+    out_spec = a_spec if use_first else b_spec
+    out_dec = sp.decomp_A() if use_first else sp.decomp_B()
+    want = O.global_offsets(P, out_spec, wl, tuple(sizes)).ravel()
+    rng = np.random.default_rng(0)
+    total = int(np.prod(sizes))
+    idx = range(total) if total <= 4096 else rng.integers(0, total, 2000)
+    for g in idx:
+        coord = np.unravel_index(int(g), sizes)
+        assert out_dec.global_offset([int(x) for x in coord], wl) == want[g]
+
+
+@pytest.mark.parametrize("name", split_names())
+def test_extent_matches_reference(name):
+    m, z = split_case(name)
+    c, S = _shape(m["P"], m["spec"])
+    sp = api.SplitPlan(S, 0x100000, m["work_len"], 0x200000, slab=m["mode"] if m["mode"] < 2 else 0,
+                       B=m["B"] if m["mode"] == 2 else None)
+    assert sp.extent == int(z["info"][:, 0].max())
+    assert sp.A_factors == [int(a) for a in z["info"][0, 1:1 + len(m["shape"])]]
+
+
+def test_processor_grid_matches_reference():
+    for case in meta()["grid"]:
+        c = api.Comm(case["P"])
+        assert api.processor_grid(c, case["tasks"]) == case["grid"], case
+
+
+def test_workspace_too_small_rejected():
+    c, S = _shape(4, "packed:block(16,2)|block(16,2)|local(16)")
+    with pytest.raises(api.DecompError):
+        api.SplitPlan(S, 0x1000, 2 * 1024 - 1, 0x2000)  # needs 2 * extent = 2048
+
+
+def test_invalid_factor_rejected():
+    c, S = _shape(4, "packed:block(16,2)|block(16,2)|local(16)")
+    with pytest.raises(api.DecompError):
+        api.SplitPlan(S, 0x1000, 4096, 0x2000, B=[3, 4, 4])
+
+
+def test_reference_descriptor_and_exact_descriptor():
+    """getTransformed is the reference's factor_reverse(A,B) over B; it agrees with the exact
+    descriptor when A == B and differs otherwise (the reference's defect)."""
+    for spec, same in [("packed:block(16,2)|block(16,2)|local(16)", True),
+                       ("packed:local(8)|block(12,2)|block(16,2)", False)]:
+        c, S = _shape(4, spec)
+        sp = api.SplitPlan(S, 0x1000, 8192, 0x2000)
+        ref = sp.transformed()
+        ex = sp.transformed_exact()
+        sizes = [16, 16, 16] if same else [8, 12, 16]
+        diff = 0
+        for g in range(int(np.prod(sizes))):
+            coord = [int(x) for x in np.unravel_index(g, sizes)]
+            diff += ref.global_offset(coord, 8192) != ex.global_offset(coord, 8192)
+        assert (diff == 0) == same
+
+
+def test_gcd():
+    lib = api.load()
+    for u, v in [(0, 5), (5, 0), (12, 18), (17, 5), (1 << 20, 3 << 10)]:
+        assert lib.gcd(u, v) == np.gcd(u, v)
