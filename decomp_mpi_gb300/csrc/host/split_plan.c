@@ -39,7 +39,7 @@
 #define TILE_TARGET 2048
 
 enum { LAY_START = 0, LAY_A = 1, LAY_B = 2 };
-enum { BUF_DAT = 0, BUF_WORK = 1 };
+enum { BUF_DAT = 0, BUF_WORK = 1, BUF_SCRATCH = 2 };
 
 typedef struct {
   int ranked;
@@ -75,6 +75,11 @@ struct dmg_split_impl {
   fft_layout lay[3];
   pass_rec fwd[MAXPASS], inv[MAXPASS];
   int nfwd, ninv;
+  /* the same passes with the upper-half intermediates in the fixed scratch
+   * array (per-rank pitch = ext), for dmg_split_run_noalloc */
+  fft_layout lay_s[3];
+  pass_rec fwd_s[MAXPASS], inv_s[MAXPASS];
+  size_t scratch_bytes;
   void *dev; /* one device allocation for every table */
   int dev_valid;
   void *dat, *work;
@@ -351,7 +356,10 @@ static void impl_free(struct dmg_split_impl *im) {
   if (!im) return;
   impl_free_device(im);
   if (im->events) dmg_split_destroy_events(im->events);
-  for (int k = 0; k < 3; ++k) layout_free(&im->lay[k]);
+  for (int k = 0; k < 3; ++k) {
+    layout_free(&im->lay[k]);
+    layout_free(&im->lay_s[k]);
+  }
   free(im);
 }
 
@@ -376,8 +384,8 @@ static int impl_upload(struct dmg_split_impl *im) {
   int nd = im->ndim;
   size_t cs = im->dtype == DMG_C128 ? 16 : 8;
   size_t bytes = 0;
-  fft_layout *all[3] = {&im->lay[0], &im->lay[1], &im->lay[2]};
-  for (int k = 0; k < 3; ++k) {
+  fft_layout *all[6] = {&im->lay[0], &im->lay[1], &im->lay[2], &im->lay_s[0], &im->lay_s[1], &im->lay_s[2]};
+  for (int k = 0; k < 6; ++k) {
     if (!all[k]->tab[0]) continue;
     for (int d = 0; d < nd; ++d) bytes += align256((size_t)im->L[d] * 8) + align256((size_t)im->L[d] * 4);
     if (all[k]->ranked) bytes += align256((size_t)nd * all[k]->nranks * 8);
@@ -392,7 +400,7 @@ static int impl_upload(struct dmg_split_impl *im) {
     return st;
   }
   size_t pos = 0;
-  for (int k = 0; k < 3; ++k) {
+  for (int k = 0; k < 6; ++k) {
     fft_layout *l = all[k];
     if (!l->tab[0]) continue;
     for (int d = 0; d < nd; ++d) {
@@ -459,6 +467,19 @@ static int impl_upload(struct dmg_split_impl *im) {
       for (int d = 0; d < DMG_FFT_MAXDIM; ++d) list[k].p.tw[d] = tw_dev[d];
       fill_side(&list[k].p.in, &im->lay[list[k].in_lay], nd, list[k].in_base);
       fill_side(&list[k].p.out, &im->lay[list[k].out_lay], nd, list[k].out_base);
+      /* scratch variant: an upper-half side moves to the fixed array */
+      pass_rec *sr = dir == 0 ? &im->fwd_s[k] : &im->inv_s[k];
+      *sr = list[k];
+      if (sr->in_buf == BUF_WORK && sr->in_base != 0) {
+        sr->in_buf = BUF_SCRATCH;
+        sr->in_base = 0;
+        fill_side(&sr->p.in, &im->lay_s[sr->in_lay], nd, 0);
+      }
+      if (sr->out_buf == BUF_WORK && sr->out_base != 0) {
+        sr->out_buf = BUF_SCRATCH;
+        sr->out_base = 0;
+        fill_side(&sr->p.out, &im->lay_s[sr->out_lay], nd, 0);
+      }
     }
   }
   return DMG_OK;
@@ -617,6 +638,14 @@ SplitPlan dmg_build_plan_typed(int flags, int use_first, int use_second, Decomp 
   if (layout_build(&im->lay[LAY_A], plan->A, length, "A") != DMG_OK) goto fail;
   if (!use_first && layout_build(&im->lay[LAY_B], plan->B, length, "B") != DMG_OK) goto fail;
   if (build_passes(im) != DMG_OK) goto fail;
+  /* scratch copies of the intermediate layouts: rank r's region at r * ext */
+  if (layout_build(&im->lay_s[LAY_A], plan->A, ext, "A") != DMG_OK) goto fail;
+  if (!use_first && layout_build(&im->lay_s[LAY_B], plan->B, ext, "B") != DMG_OK) goto fail;
+  {
+    int nr = im->lay_s[LAY_A].nranks;
+    if (!use_first && im->lay_s[LAY_B].nranks > nr) nr = im->lay_s[LAY_B].nranks;
+    im->scratch_bytes = (size_t)nr * (size_t)ext * (size_t)im->esize;
+  }
   plan->plan_a = (!use_second && im->nfwd > 0) ? (void *)im : NULL;
   plan->plan_b = NULL;
   for (int i = 0; i < ndim; ++i)
@@ -872,6 +901,48 @@ int dmg_split_run(SplitPlan plan, int direction, void *stream) {
 }
 
 void runSplitPlan(SplitPlan plan, int direction) { dmg_split_run(plan, direction, dmg_current_stream()); }
+
+/* ---------------------------------------------------------------- no-allocation run */
+
+size_t dmg_noalloc_scratch_bytes(void);
+int dmg_noalloc_scratch(void **ptr);
+
+/* runSplitPlan without touching the allocator: the intermediate passes live
+ * in the library's fixed device scratch array instead of the upper half of
+ * the workspace.  The plan's tables must already be on the device (one
+ * dmg_split_run uploads them).  Calls that overlap on the GPU share the one
+ * array and race. */
+int dmg_split_run_noalloc(SplitPlan plan, int direction, void *stream) {
+  if (!plan) return dmg_error(DMG_ERR_ARG, "dmg_split_run_noalloc: NULL plan");
+  struct dmg_split_impl *im = plan->impl;
+  if (direction != FFTW_FORWARD && direction != FFTW_BACKWARD)
+    return dmg_error(DMG_ERR_ARG, "dmg_split_run_noalloc: direction %d", direction);
+  if (!im->dat || !im->work) return dmg_error(DMG_ERR_ARG, "dmg_split_run_noalloc: NULL buffer");
+  if (im->scratch_bytes > dmg_noalloc_scratch_bytes())
+    return dmg_error(DMG_ERR_BOUNDS,
+                     "dmg_split_run_noalloc: this plan needs %zu bytes of scratch (ranks x extent x element size), "
+                     "more than the fixed %zu-byte array; use runSplitPlan with a workspace instead",
+                     im->scratch_bytes, dmg_noalloc_scratch_bytes());
+  if (im->nfwd == 0)
+    return dmg_error(DMG_ERR_UNSUPPORTED, "dmg_split_run_noalloc: the plan has no transform passes");
+  if (!im->dev_valid)
+    return dmg_error(DMG_ERR_ARG,
+                     "dmg_split_run_noalloc: the plan's tables are not on the device yet; run it once with "
+                     "runSplitPlan or dmg_split_run, which uploads them");
+  void *scratch = NULL;
+  int st = dmg_noalloc_scratch(&scratch);
+  if (st != DMG_OK) return st;
+  pass_rec *list = direction == FFTW_FORWARD ? im->fwd_s : im->inv_s;
+  int cnt = direction == FFTW_FORWARD ? im->nfwd : im->ninv;
+  int dt = im->dtype == DMG_C128 ? 0 : 1;
+  for (int k = 0; k < cnt; ++k) {
+    const void *src = list[k].in_buf == BUF_DAT ? im->dat : list[k].in_buf == BUF_WORK ? im->work : scratch;
+    void *dst = list[k].out_buf == BUF_DAT ? im->dat : list[k].out_buf == BUF_WORK ? im->work : scratch;
+    st = dmg_fft_pass_launch(&list[k].p, dt, src, dst, stream);
+    if (st != DMG_OK) return st;
+  }
+  return DMG_OK;
+}
 
 /* ---------------------------------------------------------------- visitor */
 

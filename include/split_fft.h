@@ -152,6 +152,29 @@ int dmg_split_pass_times(SplitPlan plan, int direction, float *ms, int max);
 /** Short description of the pass list. */
 const char *dmg_split_describe(SplitPlan plan);
 
+/** runSplitPlan for callers that cannot allocate device memory when they
+ * run the transform: code inside a region that a CUDA graph is capturing, a
+ * real-time loop that must not wait on the allocator, or an application
+ * that gives all of HBM to its own pool.  It has no counterpart in the
+ * reference (whose MPI ranks always own their workspace).
+ *
+ * The intermediate passes use a fixed device array of 64 MiB that the
+ * library holds on every GPU it runs on until the process exits, instead of
+ * the upper half of each rank's workspace; `dat` and the B-layout output in
+ * the workspace's lower half are the caller's buffers as usual.  The call
+ * allocates nothing: the plan's address tables must already be on the
+ * device (any earlier dmg_split_run / runSplitPlan of the plan uploads
+ * them, otherwise the call returns DMG_ERR_ARG), and plans needing more
+ * than 64 MiB of scratch (virtual ranks x extent x element size) are
+ * rejected with DMG_ERR_BOUNDS.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress); make that first call
+ * before any stream capture.  Every call uses the same array and the
+ * passes overwrite whatever an earlier call left there; calls that overlap
+ * on the GPU (different streams, no ordering) race on it. */
+int dmg_split_run_noalloc(SplitPlan plan, int direction, void *stream);
+/** Size in bytes of the fixed scratch array used by dmg_split_run_noalloc. */
+size_t dmg_noalloc_scratch_bytes(void);
+
 /** Processor grid over the communicator's ranks for `ndim` task counts
  * (reference processor_grid.c:73-97); the caller frees the result. */
 int *makeProcessorGrid(MPI_Comm comm, int ndim, int tasks[]);
