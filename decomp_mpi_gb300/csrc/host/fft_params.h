@@ -41,11 +41,20 @@ struct dmg_fft_pass {
   int64_t ntiles;
   int32_t load_order[3];       /* tile axes (0 = t, 1 = v1, 2 = v2), fastest first */
   int32_t store_order[3];
+  /* the same geometry in the form the kernel uses without indexing arrays:
+   * for tile axis k (0 t, 1 v1, 2 v2): the dimension it belongs to (-1 when
+   * absent) and whether it is the z sub-axis; and its position (0 fastest,
+   * 1, 2 slowest) in the load and the store orders */
+  int32_t kdim[3], kisz[3];
+  int32_t load_pos[3], store_pos[3];
   int32_t nfac;
   int32_t fac[DMG_FFT_MAXFAC]; /* radices, first stage first */
   const void *roots;           /* n roots exp(-2 pi i k / n), double2 or float2 */
   int32_t sign;                /* -1 forward, +1 inverse */
-  int32_t twiddle;             /* 0 none, 1 multiply after the transform, 2 multiply by the conjugate before */
+  /* split twiddle of the transformed dimension d = t/2 (t a z sub-axis):
+   * 0 none; 1 multiply after the transform by exp(-2 pi i y_d k_d / L_d);
+   * 2 multiply by its conjugate before the transform */
+  int32_t twiddle;
   const void *tw[DMG_FFT_MAXDIM]; /* per dim: L_d roots exp(-2 pi i m / L_d) */
   struct dmg_fft_layout in, out;
 };

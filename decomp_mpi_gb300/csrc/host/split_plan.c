@@ -36,7 +36,7 @@
 #endif
 
 #define MAXPASS (2 * DMG_FFT_MAXDIM)
-#define TILE_TARGET 2048
+#define TILE_TARGET 1024
 
 enum { LAY_START = 0, LAY_A = 1, LAY_B = 2 };
 enum { BUF_DAT = 0, BUF_WORK = 1, BUF_SCRATCH = 2 };
@@ -317,6 +317,15 @@ static int pass_geometry(const struct dmg_split_impl *im, struct dmg_fft_pass *p
   so[2] = p->v2 >= 0 ? sub_step(im, lo, p->v2) : INT64_MAX;
   order_by_step(si, p->load_order);
   order_by_step(so, p->store_order);
+  const int axes[3] = {t, p->v1, p->v2};
+  for (int k = 0; k < 3; ++k) {
+    p->kdim[k] = axes[k] >= 0 ? axes[k] / 2 : -1;
+    p->kisz[k] = axes[k] >= 0 ? (axes[k] & 1) : 0;
+  }
+  for (int i = 0; i < 3; ++i) {
+    p->load_pos[p->load_order[i]] = i;
+    p->store_pos[p->store_order[i]] = i;
+  }
   return DMG_OK;
 }
 
@@ -522,7 +531,10 @@ static int build_passes(struct dmg_split_impl *im) {
     int st = pass_geometry(im, &f->p, subs[k], &im->lay[in_lay], &im->lay[out_lay]);
     if (st != DMG_OK) return st;
     f->p.sign = -1;
-    f->p.twiddle = (k == n1 - 1 && n1 > 0 && K > n1) ? 1 : 0;
+    /* each stage-1 pass applies its own dimension's factor exp(-2 pi i y_d k1_d / L_d)
+     * after its transform; the factor is constant along the other dimensions'
+     * lines, so it commutes with the remaining stage-1 passes */
+    f->p.twiddle = (stage[k] == 1 && K > n1 && im->A[subs[k] / 2] > 1) ? 1 : 0;
   }
   for (int k = 0; k < K; ++k) {
     /* inverse pass k undoes forward pass K-1-k: it reads what that pass

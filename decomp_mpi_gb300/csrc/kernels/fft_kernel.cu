@@ -21,7 +21,7 @@
 
 namespace {
 
-constexpr int NT = 256;
+constexpr int NT = 128;
 constexpr int TILE_MAX = 4096;  // complex values per tile buffer (one 4096-long line at most)
 
 template <typename T>
@@ -115,45 +115,56 @@ __device__ __forceinline__ void dft5(C2<T> *a) {
   a[3] = sub<T>(p2, q2);
 }
 
-struct AddrCtx {
-  int ndim;
-};
-
 template <typename T>
 __device__ __forceinline__ int64_t layout_addr(const dmg_fft_layout &L, int ndim, const int *x) {
   if (!L.ranked) {
     int64_t a = L.base;
-    for (int d = 0; d < ndim; ++d) a += __ldg(L.tab[d] + x[d]);
+#pragma unroll
+    for (int d = 0; d < DMG_FFT_MAXDIM; ++d)
+      if (d < ndim) a += __ldg(L.tab[d] + x[d]);
     return a;
   }
   int32_t R = 0;
-  for (int d = 0; d < ndim; ++d) R += __ldg(L.rk[d] + x[d]);
+#pragma unroll
+  for (int d = 0; d < DMG_FFT_MAXDIM; ++d)
+    if (d < ndim) R += __ldg(L.rk[d] + x[d]);
   int64_t a = L.base + (int64_t)R * L.pitch;
-  for (int d = 0; d < ndim; ++d) a += __ldg(L.tab[d] + x[d]) * __ldg(L.rstride + (size_t)d * L.nranks + R);
+#pragma unroll
+  for (int d = 0; d < DMG_FFT_MAXDIM; ++d)
+    if (d < ndim) a += __ldg(L.tab[d] + x[d]) * __ldg(L.rstride + (size_t)d * L.nranks + R);
   return a;
 }
 
-// split twiddle prod_d w_{L_d}^{y_d * z_d} (conjugated when conj)
-template <typename T>
-__device__ __forceinline__ C2<T> split_twiddle(const dmg_fft_pass &p, const int *sc, bool conj) {
-  C2<T> w = mk<T>((T)1, (T)0);
-  for (int d = 0; d < p.ndim; ++d) {
-    int e = sc[2 * d] * sc[2 * d + 1];  // y_d * z_d < L_d
-    if (e == 0) continue;
-    C2<T> f = reinterpret_cast<const C2<T> *>(p.tw[d])[e];
-    w = mul<T>(w, f);
-  }
-  if (conj) w.y = -w.y;
-  return w;
+// Tile-axis coordinates (c0 = t, c1 = v1, c2 = v2) of a linear index e in an
+// order given by each axis's position (0 fastest); selects, no indexing.
+__device__ __forceinline__ void tile_coords(int e, const int32_t *pos, int n0, int n1, int n2, int &c0, int &c1,
+                                            int &c2) {
+  // extents in order: fast, mid
+  const int ef = pos[0] == 0 ? n0 : pos[1] == 0 ? n1 : n2;
+  const int em = pos[0] == 1 ? n0 : pos[1] == 1 ? n1 : n2;
+  const int i_f = e % ef;
+  const int rest = e / ef;
+  const int i_m = rest % em;
+  const int i_s = rest / em;
+  c0 = pos[0] == 0 ? i_f : pos[0] == 1 ? i_m : i_s;
+  c1 = pos[1] == 0 ? i_f : pos[1] == 1 ? i_m : i_s;
+  c2 = pos[2] == 0 ? i_f : pos[2] == 1 ? i_m : i_s;
 }
 
-// decompose a linear tile index in the given order (fastest first)
-__device__ __forceinline__ void tile_coords(int e, const int32_t *order, const int *ext, int *c) {
-  int o0 = order[0], o1 = order[1], o2 = order[2];
-  c[o0] = e % ext[o0];
-  e /= ext[o0];
-  c[o1] = e % ext[o1];
-  c[o2] = e / ext[o1];
+// Global coordinates x_d of the element at tile offsets (c0, c1, c2).
+__device__ __forceinline__ void element_x(const dmg_fft_pass &p, const int *yb, const int *zb, int c0, int c1, int c2,
+                                          int *x) {
+#pragma unroll
+  for (int d = 0; d < DMG_FFT_MAXDIM; ++d) {
+    int y = yb[d], z = zb[d];
+    y += (p.kdim[0] == d && !p.kisz[0]) ? c0 : 0;
+    z += (p.kdim[0] == d && p.kisz[0]) ? c0 : 0;
+    y += (p.kdim[1] == d && !p.kisz[1]) ? c1 : 0;
+    z += (p.kdim[1] == d && p.kisz[1]) ? c1 : 0;
+    y += (p.kdim[2] == d && !p.kisz[2]) ? c2 : 0;
+    z += (p.kdim[2] == d && p.kisz[2]) ? c2 : 0;
+    x[d] = y + p.A[d] * z;
+  }
 }
 
 template <typename T, int SIGN>
@@ -175,51 +186,69 @@ __global__ void __launch_bounds__(NT) fft_pass_kernel(const dmg_fft_pass p, cons
       roots[i] = w;
     }
   }
-  __shared__ int s_sc[6];
-  __shared__ int s_lim[3];
+  __shared__ int s_yb[DMG_FFT_MAXDIM], s_zb[DMG_FFT_MAXDIM];
+  __shared__ int s_lim1, s_lim2, s_ytw;
+  // the transformed dimension and, for its twiddle, which vector axes carry its y
+  const int td = p.t >> 1;
+  const C2<T> *twt = reinterpret_cast<const C2<T> *>(p.tw[td]);
+  const bool v1_ytd = p.kdim[1] == td && !p.kisz[1];
+  const bool v2_ytd = p.kdim[2] == td && !p.kisz[2];
 
   for (int64_t tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
     __syncthreads();
     if (tid == 0) {
       int64_t t = tile;
-      int sc[6] = {0, 0, 0, 0, 0, 0};
-      int i1 = (int)(t % p.nt1);
+      const int i1 = (int)(t % p.nt1);
       t /= p.nt1;
-      int i2 = (int)(t % p.nt2);
+      const int i2 = (int)(t % p.nt2);
       t /= p.nt2;
+      for (int d = 0; d < DMG_FFT_MAXDIM; ++d) s_yb[d] = s_zb[d] = 0;
       for (int b = 0; b < p.nbatch; ++b) {
-        sc[p.bsub[b]] = (int)(t % p.blen[b]);
+        const int c = (int)(t % p.blen[b]);
         t /= p.blen[b];
+        const int s = p.bsub[b];
+        if (s & 1) s_zb[s >> 1] += c;
+        else s_yb[s >> 1] += c;
       }
-      if (p.v1 >= 0) sc[p.v1] = i1 * p.M1;
-      if (p.v2 >= 0) sc[p.v2] = i2 * p.M2;
-      for (int s = 0; s < 6; ++s) s_sc[s] = sc[s];
-      s_lim[0] = n;
-      s_lim[1] = p.v1 >= 0 ? min(p.M1, p.nv1 - i1 * p.M1) : 1;
-      s_lim[2] = p.v2 >= 0 ? min(p.M2, p.nv2 - i2 * p.M2) : 1;
+      if (p.v1 >= 0) {
+        if (p.v1 & 1) s_zb[p.v1 >> 1] += i1 * p.M1;
+        else s_yb[p.v1 >> 1] += i1 * p.M1;
+      }
+      if (p.v2 >= 0) {
+        if (p.v2 & 1) s_zb[p.v2 >> 1] += i2 * p.M2;
+        else s_yb[p.v2 >> 1] += i2 * p.M2;
+      }
+      s_ytw = s_yb[td];
+      s_lim1 = p.v1 >= 0 ? min(p.M1, p.nv1 - i1 * p.M1) : 1;
+      s_lim2 = p.v2 >= 0 ? min(p.M2, p.nv2 - i2 * p.M2) : 1;
     }
     __syncthreads();
-    int base[6];
+    int yb[DMG_FFT_MAXDIM], zb[DMG_FFT_MAXDIM];
 #pragma unroll
-    for (int s = 0; s < 6; ++s) base[s] = s_sc[s];
-    const int ext[3] = {s_lim[0], s_lim[1], s_lim[2]};
-    const int total = ext[0] * ext[1] * ext[2];
+    for (int d = 0; d < DMG_FFT_MAXDIM; ++d) {
+      yb[d] = s_yb[d];
+      zb[d] = s_zb[d];
+    }
+    const int lim1 = s_lim1, lim2 = s_lim2, ytw = s_ytw;
+    const int total = n * lim1 * lim2;
 
     // ---- gather from the input layout ----
     for (int e = tid; e < total; e += NT) {
-      int c[3];
-      tile_coords(e, p.load_order, ext, c);
-      int sc[6];
-#pragma unroll
-      for (int s = 0; s < 6; ++s) sc[s] = base[s];
-      sc[p.t] = c[0];
-      if (p.v1 >= 0) sc[p.v1] += c[1];
-      if (p.v2 >= 0) sc[p.v2] += c[2];
+      int c0, c1, c2;
+      tile_coords(e, p.load_pos, n, lim1, lim2, c0, c1, c2);
       int x[DMG_FFT_MAXDIM];
-      for (int d = 0; d < p.ndim; ++d) x[d] = sc[2 * d] + p.A[d] * sc[2 * d + 1];
+      element_x(p, yb, zb, c0, c1, c2, x);
       C2<T> v = src[layout_addr<T>(p.in, p.ndim, x)];
-      if (p.twiddle == 2) v = mul<T>(v, split_twiddle<T>(p, sc, true));
-      bufA[(size_t)(c[1] + p.M1 * c[2]) * ld + c[0]] = v;
+      if (p.twiddle == 2) {
+        const int yv = ytw + (v1_ytd ? c1 : 0) + (v2_ytd ? c2 : 0);
+        const int ex = yv * c0;
+        if (ex) {
+          C2<T> w = twt[ex];
+          w.y = -w.y;
+          v = mul<T>(v, w);
+        }
+      }
+      bufA[(size_t)(c1 + p.M1 * c2) * ld + c0] = v;
     }
     __syncthreads();
 
@@ -262,14 +291,21 @@ __global__ void __launch_bounds__(NT) fft_pass_kernel(const dmg_fft_pass p, cons
             dft3<T, SIGN>(a);
           } else if (r == 5) {
             dft5<T, SIGN>(a);
-          } else {  // 6, 7: direct
+          } else {  // 7: direct, fully unrolled so that a[] stays in registers
             C2<T> y[8];
-            for (int s = 0; s < r; ++s) {
-              C2<T> acc = a[0];
-              for (int q = 1; q < r; ++q) acc = add<T>(acc, mul<T>(a[q], roots[((q * s) % r) * nr]));
-              y[s] = acc;
+#pragma unroll
+            for (int s = 0; s < 8; ++s) {
+              if (s < r) {
+                C2<T> acc = a[0];
+#pragma unroll
+                for (int q = 1; q < 8; ++q)
+                  if (q < r) acc = add<T>(acc, mul<T>(a[q], roots[((q * s) % r) * nr]));
+                y[s] = acc;
+              }
             }
-            for (int s = 0; s < r; ++s) a[s] = y[s];
+#pragma unroll
+            for (int s = 0; s < 8; ++s)
+              if (s < r) a[s] = y[s];
           }
 #pragma unroll
           for (int s = 0; s < 8; ++s)
@@ -296,18 +332,16 @@ __global__ void __launch_bounds__(NT) fft_pass_kernel(const dmg_fft_pass p, cons
 
     // ---- scatter to the output layout ----
     for (int e = tid; e < total; e += NT) {
-      int c[3];
-      tile_coords(e, p.store_order, ext, c);
-      int sc[6];
-#pragma unroll
-      for (int s = 0; s < 6; ++s) sc[s] = base[s];
-      sc[p.t] = c[0];
-      if (p.v1 >= 0) sc[p.v1] += c[1];
-      if (p.v2 >= 0) sc[p.v2] += c[2];
-      C2<T> v = in[(size_t)(c[1] + p.M1 * c[2]) * ld + c[0]];
-      if (p.twiddle == 1) v = mul<T>(v, split_twiddle<T>(p, sc, false));
+      int c0, c1, c2;
+      tile_coords(e, p.store_pos, n, lim1, lim2, c0, c1, c2);
+      C2<T> v = in[(size_t)(c1 + p.M1 * c2) * ld + c0];
+      if (p.twiddle == 1) {
+        const int yv = ytw + (v1_ytd ? c1 : 0) + (v2_ytd ? c2 : 0);
+        const int ex = yv * c0;
+        if (ex) v = mul<T>(v, twt[ex]);
+      }
       int x[DMG_FFT_MAXDIM];
-      for (int d = 0; d < p.ndim; ++d) x[d] = sc[2 * d] + p.A[d] * sc[2 * d + 1];
+      element_x(p, yb, zb, c0, c1, c2, x);
       dst[layout_addr<T>(p.out, p.ndim, x)] = v;
     }
   }
