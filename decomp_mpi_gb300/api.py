@@ -24,6 +24,9 @@ FFTW_FORWARD = -1
 FFTW_BACKWARD = 1
 C128 = 0
 C64 = 1
+ARITH_FP64 = 0
+ARITH_FP32 = 1
+ARITH_DF = 2
 
 
 class _DecompStruct(ctypes.Structure):
@@ -343,7 +346,7 @@ class SplitPlan:
     """
 
     def __init__(self, start: Decomp, dat_ptr: int, length: int, work_ptr: int, slab: int = 0, B=None,
-                 dtype: int = C128, autotune: bool = False):
+                 dtype: int = C128, autotune: bool = False, arith=None):
         self.lib = load()
         self.start = start
         if autotune:
@@ -361,6 +364,16 @@ class SplitPlan:
         self.h = h
         self.length = int(length)
         self.dtype = dtype
+        if arith is not None:
+            self.set_arith(arith)
+
+    def set_arith(self, arith):
+        """ARITH_DF (default for complex128) or ARITH_FP64; complex64 plans are ARITH_FP32."""
+        check(self.lib.dmg_split_set_arith(self.h, int(arith)), "dmg_split_set_arith")
+
+    @property
+    def arith(self):
+        return self.lib.dmg_split_get_arith(self.h)
 
     @property
     def _s(self):

@@ -56,14 +56,24 @@ struct dmg_fft_pass {
    * 2 multiply by its conjugate before the transform */
   int32_t twiddle;
   const void *tw[DMG_FFT_MAXDIM]; /* per dim: L_d roots exp(-2 pi i m / L_d) */
+  /* double-float passes (dtype 2): whether the input / output is stored as
+   * complex128 (converted at load / store, scaled by 2^-E / 2^E) rather
+   * than as double-float pairs; E = *scale_exp */
+  int32_t in_fp64, out_fp64;
+  const int32_t *scale_exp;
   struct dmg_fft_layout in, out;
 };
 
 #ifdef __cplusplus
 extern "C" {
 #endif
-/* dtype 0: complex128 (FP64), 1: complex64 (FP32). */
+/* dtype 0: complex128 in FP64 arithmetic, 1: complex64 in FP32, 2: complex128
+ * data in double-float (FP32 pair) arithmetic. */
 int dmg_fft_pass_launch(const struct dmg_fft_pass *p, int dtype, const void *src, void *dst, void *stream);
+/* Largest biased FP64 exponent of max(|re|, |im|) over the N = prod(L)
+ * complex128 elements of a layout, into *out (which the call first sets to 0). */
+int dmg_fft_maxexp_launch(const struct dmg_fft_layout *lay, int ndim, const int32_t *A, const int32_t *L,
+                          const void *src, int32_t *out, void *stream);
 /* Shared memory bytes a pass needs. */
 size_t dmg_fft_pass_smem(const struct dmg_fft_pass *p, int dtype);
 #ifdef __cplusplus

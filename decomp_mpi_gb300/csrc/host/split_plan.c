@@ -63,6 +63,8 @@ typedef struct {
 
 struct dmg_split_impl {
   int dtype; /* DMG_C128 or DMG_C64 */
+  int arith; /* DMG_ARITH_FP64, DMG_ARITH_DF (complex128) or DMG_ARITH_FP32 (complex64) */
+  int32_t *d_scale; /* device int: largest input exponent (double-float runs) */
   int esize; /* bytes per element */
   int ndim;
   int A[DMG_FFT_MAXDIM], B[DMG_FFT_MAXDIM], L[DMG_FFT_MAXDIM];
@@ -401,6 +403,7 @@ static int impl_upload(struct dmg_split_impl *im) {
   }
   for (int k = 0; k < im->nfwd; ++k) bytes += align256((size_t)im->fwd[k].p.n * cs);
   for (int d = 0; d < nd; ++d) bytes += align256((size_t)im->L[d] * cs);
+  bytes += 256; /* scale exponent */
   char *host = (char *)calloc(1, bytes + 256);
   void *dev = NULL;
   int st = dmg_dev_alloc(&dev, bytes + 256);
@@ -432,7 +435,16 @@ static int impl_upload(struct dmg_split_impl *im) {
     for (int i = 0; i < n; ++i) {
       /* exp(-2 pi i k / n), evaluated in long double and rounded once */
       long double a = -2.0L * 3.141592653589793238462643383279502884L * (long double)i / (long double)n;
-      if (cs == 16) {
+      if (im->arith == DMG_ARITH_DF) {
+        /* double-float: each component as hi + lo floats */
+        long double c = cosl(a), sn = sinl(a);
+        float ch = (float)c, sh = (float)sn;
+        float *f = (float *)(host + pos) + 4 * i;
+        f[0] = ch;
+        f[1] = (float)(c - (long double)ch);
+        f[2] = sh;
+        f[3] = (float)(sn - (long double)sh);
+      } else if (cs == 16) {
         ((double *)(host + pos))[2 * i] = (double)cosl(a);
         ((double *)(host + pos))[2 * i + 1] = (double)sinl(a);
       } else {
@@ -448,7 +460,13 @@ static int impl_upload(struct dmg_split_impl *im) {
     for (int m = 0; m < im->L[d]; ++m) {
       double re, iv;
       twiddle_value(m, im->L[d], &re, &iv);
-      if (cs == 16) {
+      if (im->arith == DMG_ARITH_DF) {
+        float *f = (float *)(host + pos) + 4 * m;
+        f[0] = (float)re;
+        f[1] = (float)(re - (double)f[0]);
+        f[2] = (float)iv;
+        f[3] = (float)(iv - (double)f[2]);
+      } else if (cs == 16) {
         ((double *)(host + pos))[2 * m] = re;
         ((double *)(host + pos))[2 * m + 1] = iv;
       } else {
@@ -459,6 +477,8 @@ static int impl_upload(struct dmg_split_impl *im) {
     tw_dev[d] = (char *)dev + pos;
     pos += align256((size_t)im->L[d] * cs);
   }
+  im->d_scale = (int32_t *)((char *)dev + pos);
+  pos += 256;
   st = dmg_dev_upload(dev, host, pos);
   free(host);
   if (st != DMG_OK) {
@@ -474,6 +494,11 @@ static int impl_upload(struct dmg_split_impl *im) {
       int fk = dir == 0 ? k : im->nfwd - 1 - k; /* the inverse mirrors the forward list */
       list[k].p.roots = roots_dev[fk];
       for (int d = 0; d < DMG_FFT_MAXDIM; ++d) list[k].p.tw[d] = tw_dev[d];
+      /* double-float runs keep float pairs between passes: only the first
+       * pass reads complex128 and only the last writes it */
+      list[k].p.in_fp64 = im->arith == DMG_ARITH_DF && k == 0;
+      list[k].p.out_fp64 = im->arith == DMG_ARITH_DF && k == cnt - 1;
+      list[k].p.scale_exp = im->d_scale;
       fill_side(&list[k].p.in, &im->lay[list[k].in_lay], nd, list[k].in_base);
       fill_side(&list[k].p.out, &im->lay[list[k].out_lay], nd, list[k].out_base);
       /* scratch variant: an upper-half side moves to the fixed array */
@@ -564,6 +589,21 @@ static int build_passes(struct dmg_split_impl *im) {
   return DMG_OK;
 }
 
+/* kernel dtype of a plan's arithmetic */
+static int arith_dtype(const struct dmg_split_impl *im) {
+  return im->arith == DMG_ARITH_FP64 ? 0 : im->arith == DMG_ARITH_FP32 ? 1 : 2;
+}
+
+/* largest exponent of the run's complex128 input, for the double-float scaling */
+static int launch_maxexp(struct dmg_split_impl *im, const pass_rec *first, const void *src, void *stream) {
+  int32_t L[DMG_FFT_MAXDIM], A[DMG_FFT_MAXDIM];
+  for (int d = 0; d < DMG_FFT_MAXDIM; ++d) {
+    L[d] = im->L[d];
+    A[d] = im->A[d];
+  }
+  return dmg_fft_maxexp_launch(&first->p.in, im->ndim, A, L, src, im->d_scale, stream);
+}
+
 /* ---------------------------------------------------------------- public API */
 
 SplitPlan dmg_build_plan_typed(int flags, int use_first, int use_second, Decomp start, int ndim, int A[], int B[],
@@ -597,6 +637,7 @@ SplitPlan dmg_build_plan_typed(int flags, int use_first, int use_second, Decomp 
   plan->src = (fftw_complex *)dat;
   plan->work = (fftw_complex *)workspace;
   im->dtype = dtype;
+  im->arith = dtype == DMG_C128 ? DMG_ARITH_DF : DMG_ARITH_FP32;
   im->esize = dtype == DMG_C128 ? 16 : 8;
   im->ndim = ndim;
   im->use_first = use_first;
@@ -820,9 +861,24 @@ int dmg_split_set_dat_pitch(SplitPlan plan, long long pitch) {
   return dmg_reshape_set_pitch(plan->start_to_A, pitch, 0) | dmg_reshape_set_pitch(plan->A_to_start, 0, pitch);
 }
 
+int dmg_split_set_arith(SplitPlan plan, int arith) {
+  if (!plan) return dmg_error(DMG_ERR_ARG, "dmg_split_set_arith: NULL plan");
+  struct dmg_split_impl *im = plan->impl;
+  if (im->dtype == DMG_C64 ? arith != DMG_ARITH_FP32 : (arith != DMG_ARITH_FP64 && arith != DMG_ARITH_DF))
+    return dmg_error(DMG_ERR_ARG, "dmg_split_set_arith: arithmetic %d does not apply to this element type", arith);
+  if (arith != im->arith) {
+    im->arith = arith;
+    impl_free_device(im); /* tables differ between arithmetics */
+  }
+  return DMG_OK;
+}
+
+int dmg_split_get_arith(SplitPlan plan) { return plan ? plan->impl->arith : -1; }
+
 int dmg_split_launches(SplitPlan plan, int direction) {
   if (!plan) return 0;
   int k = direction == FFTW_FORWARD ? plan->impl->nfwd : plan->impl->ninv;
+  if (k > 0 && plan->impl->arith == DMG_ARITH_DF) k += 1; /* the exponent pre-pass */
   return k > 0 ? k : 1;
 }
 
@@ -894,7 +950,11 @@ int dmg_split_run(SplitPlan plan, int direction, void *stream) {
   }
   pass_rec *list = direction == FFTW_FORWARD ? im->fwd : im->inv;
   int cnt = direction == FFTW_FORWARD ? im->nfwd : im->ninv;
-  int dt = im->dtype == DMG_C128 ? 0 : 1;
+  int dt = arith_dtype(im);
+  if (im->arith == DMG_ARITH_DF) {
+    int st = launch_maxexp(im, &list[0], list[0].in_buf == BUF_DAT ? im->dat : im->work, stream);
+    if (st != DMG_OK) return st;
+  }
   if (im->timing) {
     if (im->timed_passes > 0 && !im->collected) dmg_split_collect_times(plan);
     im->timed_dir = direction;
@@ -946,7 +1006,11 @@ int dmg_split_run_noalloc(SplitPlan plan, int direction, void *stream) {
   if (st != DMG_OK) return st;
   pass_rec *list = direction == FFTW_FORWARD ? im->fwd_s : im->inv_s;
   int cnt = direction == FFTW_FORWARD ? im->nfwd : im->ninv;
-  int dt = im->dtype == DMG_C128 ? 0 : 1;
+  int dt = arith_dtype(im);
+  if (im->arith == DMG_ARITH_DF) {
+    st = launch_maxexp(im, &list[0], list[0].in_buf == BUF_DAT ? im->dat : im->work, stream);
+    if (st != DMG_OK) return st;
+  }
   for (int k = 0; k < cnt; ++k) {
     const void *src = list[k].in_buf == BUF_DAT ? im->dat : list[k].in_buf == BUF_WORK ? im->work : scratch;
     void *dst = list[k].out_buf == BUF_DAT ? im->dat : list[k].out_buf == BUF_WORK ? im->work : scratch;

@@ -20,9 +20,9 @@
  * transform (unnormalised, FFTW convention): it reads the B-layout data in
  * the workspace and writes N times the original into `dat`.
  *
- * The device arithmetic is FP64 complex (complex128) unless the plan was
- * made for complex64 (dmg_makeSplitPlanTyped).  No FFTW, cuFFT or CPU code
- * runs: every pass is a hand-written sm_103a kernel.
+ * Data is complex128 unless the plan was made for complex64
+ * (dmg_makeSplitPlanTyped); see DMG_ARITH_* for the arithmetic.  No FFTW,
+ * cuFFT or CPU code runs: every pass is a hand-written sm_103a kernel.
  */
 #include "reshape.h"
 
@@ -130,6 +130,19 @@ SplitPlan dmg_makeSplitPlanTyped(int slab, Decomp start, void *dat, long long le
 /** makeParallelPlan for a given element type. */
 SplitPlan dmg_makeParallelPlanTyped(Decomp start, int *initial_factor, void *dat, long long length,
                                     void *workspace, int dtype);
+/* Arithmetic of the device passes.  complex128 plans run in double-float by
+ * default: each real is an unevaluated sum of two floats (48-bit
+ * significand, relative error around 1e-14 on a 512^3 transform), computed
+ * on the FP32 pipes; the input is scaled by a power of two so any FP64
+ * magnitude fits.  DMG_ARITH_FP64 computes in native FP64 instead (GB300's
+ * FP64 rate is about 1/56 of its FP32 rate).  complex64 plans use FP32. */
+#define DMG_ARITH_FP64 0
+#define DMG_ARITH_FP32 1
+#define DMG_ARITH_DF 2
+/** Select the arithmetic of a plan (DMG_ARITH_FP64 or DMG_ARITH_DF for
+ * complex128; complex64 plans accept only DMG_ARITH_FP32). */
+int dmg_split_set_arith(SplitPlan plan, int arith);
+int dmg_split_get_arith(SplitPlan plan);
 /** Status-returning run on an explicit stream (NULL = legacy default). */
 int dmg_split_run(SplitPlan plan, int direction, void *stream);
 /** Rebind the device buffers of a plan (same sizes). */

@@ -13,13 +13,19 @@ TOL_C64 = 2e-6    # relative L2, FP32
 
 
 def _rel(a, b):
-    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    # scaled by the largest magnitude first, so that values near the ends of
+    # the FP64 range neither overflow nor underflow the norms
+    m = float(np.max(np.abs(b)))
+    if m == 0.0:
+        return float(np.max(np.abs(a)))
+    return float(np.linalg.norm((a - b) / m) / np.linalg.norm(b / m))
 
 
 class Run:
     """One split plan on the GPU with its buffers."""
 
-    def __init__(self, P, spec, shape, cuda, mode=0, B=None, dtype=api.C128, work_len=None, seed=0):
+    def __init__(self, P, spec, shape, cuda, mode=0, B=None, dtype=api.C128, work_len=None, seed=0, arith=None,
+                 scale=1.0):
         import torch
         self.torch = torch
         self.P, self.spec, self.shape = P, spec, tuple(shape)
@@ -28,14 +34,15 @@ class Run:
         self.dp = self.S.extent()
         self.wl = work_len or 2 * int(np.prod(shape))
         rng = np.random.default_rng(seed)
-        self.glob = rng.uniform(-1, 1, self.shape) + 1j * rng.uniform(-1, 1, self.shape)
+        self.glob = (rng.uniform(-1, 1, self.shape) + 1j * rng.uniform(-1, 1, self.shape)) * scale
         tdt = torch.complex128 if dtype == api.C128 else torch.complex64
         self.npdt = np.complex128 if dtype == api.C128 else np.complex64
         host = O.scatter_global(P, spec, self.glob, self.dp).astype(self.npdt)
         self.dat = torch.from_numpy(host).to(cuda)
         self.work = torch.zeros(P * self.wl, dtype=tdt, device=cuda)
         self.plan = api.SplitPlan(self.S, self.dat.data_ptr(), self.wl, self.work.data_ptr(),
-                                  slab=mode if mode < 2 else 0, B=B if mode == 2 else None, dtype=dtype)
+                                  slab=mode if mode < 2 else 0, B=B if mode == 2 else None, dtype=dtype,
+                                  arith=arith)
         self.mode, self.B = mode, B
         self.stream = torch.cuda.current_stream(cuda).cuda_stream
 
@@ -137,3 +144,46 @@ def test_linear_index_pattern_roundtrip(cuda):
     back = r.inverse()
     g = O.gather_global(P, spec, back, r.dp, (L, L, L)) / L ** 3
     assert np.max(np.abs(g - glob)) < 1e-9
+
+
+@pytest.mark.parametrize("P,spec,shape,mode,B", [CASES[0], CASES[2], CASES[4], CASES[6], CASES[8], CASES[10]],
+                         ids=["64c", "48c", "14x21x11", "allA1", "1d", "frev128"])
+def test_forward_and_inverse_native_fp64(P, spec, shape, mode, B, cuda):
+    """The same transforms in native FP64 arithmetic (DMG_ARITH_FP64)."""
+    r = Run(P, spec, shape, cuda, mode, B, arith=api.ARITH_FP64)
+    assert r.plan.arith == api.ARITH_FP64
+    got = r.forward()
+    exp, mask = O.split_expected_output(P, spec, r.glob, r.wl, mode, B)
+    assert _rel(got[mask], exp[mask]) < TOL_C128
+    back = r.inverse()
+    g = O.gather_global(P, spec, back, r.dp, r.shape) / np.prod(r.shape)
+    assert _rel(g, r.glob) < TOL_C128
+
+
+@pytest.mark.parametrize("scale", [1e300, 1e-300, 2.0 ** 600, 3e-310])
+def test_double_float_extreme_magnitudes(scale, cuda):
+    """Double-float runs scale by a power of two, so FP64 magnitudes beyond FP32's range keep their accuracy."""
+    P, spec, shape = 4, "packed:block(16,2)|block(24,2)|local(10)", (16, 24, 10)
+    r = Run(P, spec, shape, cuda, scale=scale)
+    assert r.plan.arith == api.ARITH_DF
+    got = r.forward()
+    exp, mask = O.split_expected_output(P, spec, r.glob, r.wl)
+    if scale < 1e-307:  # denormal inputs: accuracy relative to the largest value
+        assert np.max(np.abs(got[mask] - exp[mask])) <= 1e-12 * np.max(np.abs(exp[mask])) + 1e-320
+        return
+    assert np.all(np.isfinite(got[mask]))
+    assert _rel(got[mask], exp[mask]) < TOL_C128
+    back = r.inverse()
+    g = O.gather_global(P, spec, back, r.dp, r.shape) / np.prod(r.shape)
+    assert _rel(g, r.glob) < TOL_C128
+
+
+def test_double_float_zero_input(cuda):
+    import torch
+    P, spec, shape = 4, "packed:block(8,2)|block(8,2)|local(8)", (8, 8, 8)
+    r = Run(P, spec, shape, cuda)
+    r.dat.zero_()
+    got = r.forward()
+    assert not np.any(got)
+    assert r.plan.arith == api.ARITH_DF
+    del torch
