@@ -230,6 +230,25 @@ def run_gpu(args):
             nat_fwd.append(ev[1].elapsed_time(ev[2]))
             nat_inv.append(ev[2].elapsed_time(ev[3]))
     sp.set_arith(api.ARITH_DF)
+    # the other pass schedule on the same plan, for comparison
+    other = api.SCHEDULE_SPLIT if sp.schedule == api.SCHEDULE_LINES else api.SCHEDULE_LINES
+    used = sp.schedule
+    alt_fwd, alt_inv = [], []
+    try:
+        sp.set_schedule(other)
+        for i in range(3):
+            ev[1].record(stream)
+            sp.run(api.FFTW_FORWARD, sh)
+            ev[2].record(stream)
+            sp.run(api.FFTW_BACKWARD, sh)
+            ev[3].record(stream)
+            torch.cuda.synchronize()
+            if i:
+                alt_fwd.append(ev[1].elapsed_time(ev[2]))
+                alt_inv.append(ev[2].elapsed_time(ev[3]))
+    except Exception:  # the other schedule does not apply to this shape
+        pass
+    sp.set_schedule(used)
 
     # correctness of this run: forward then inverse returns N times the input
     r01.run(a0.data_ptr(), a1.data_ptr(), sh)
@@ -311,11 +330,15 @@ def run_gpu(args):
         "fft_pass_ms": [round(x, 3) for x in launches],
         "native_fp64_ms": {"fft_forward": round(statistics.median(nat_fwd), 3),
                            "fft_inverse": round(statistics.median(nat_inv), 3)},
+        "schedule": "lines" if used == api.SCHEDULE_LINES else "split",
+        "other_schedule_ms": ({"schedule": "lines" if other == api.SCHEDULE_LINES else "split",
+                               "fft_forward": round(statistics.median(alt_fwd), 3),
+                               "fft_inverse": round(statistics.median(alt_inv), 3)} if alt_fwd else None),
         "roundtrip_rel_l2": rt_err,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                      "traffic": ncu_traffic("fft_pass_512c128"),
-                     "kernel": "fft_pass_kernel<df> (one double-float split-FFT pass: 2*N*16 B algorithmic)",
+                     "kernel": "fft_pass_kernel<df> (one double-float FFT pass over the array: 2*N*16 B algorithmic)",
                      "fp64_equivalent": {"achieved_tflops": round(pass_tflops, 3),
                                          "native_fp64_peak_tflops": round(fp64_peak, 3),
                                          "note": "5 N log2(n) flops per pass at FP64 accuracy; the native FP64 "

@@ -107,6 +107,14 @@ SIGNATURES = {
     "dmg_split_run_noalloc": (_i, [_vp, _i, _vp]),
     "dmg_split_set_arith": (_i, [_vp, _i]),
     "dmg_split_get_arith": (_i, [_vp]),
+    "dmg_split_set_schedule": (_i, [_vp, _i]),
+    "dmg_makeGlobalDecomp": (_vp, [_vp, _i, _ip]),
+    "dmg_io_gather": (_i, [_vp, _i, _vp, _vp, _vp]),
+    "dmg_io_scatter": (_i, [_vp, _i, _vp, _vp, _vp]),
+    "dmg_io_write_file": (_i, [_cp, _vp, _i, _vp, _vp]),
+    "dmg_io_read_file": (_i, [_cp, _vp, _i, _vp, _vp]),
+    "dmg_io_view": (_ll, [_vp, _i, ctypes.POINTER(_ll), ctypes.POINTER(_ll), _ll]),
+    "dmg_split_get_schedule": (_i, [_vp]),
     "dmg_noalloc_scratch_bytes": (ctypes.c_size_t, []),
 }
 

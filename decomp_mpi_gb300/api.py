@@ -27,6 +27,9 @@ C64 = 1
 ARITH_FP64 = 0
 ARITH_FP32 = 1
 ARITH_DF = 2
+SCHEDULE_AUTO = 0
+SCHEDULE_LINES = 1
+SCHEDULE_SPLIT = 2
 
 
 class _DecompStruct(ctypes.Structure):
@@ -346,7 +349,7 @@ class SplitPlan:
     """
 
     def __init__(self, start: Decomp, dat_ptr: int, length: int, work_ptr: int, slab: int = 0, B=None,
-                 dtype: int = C128, autotune: bool = False, arith=None):
+                 dtype: int = C128, autotune: bool = False, arith=None, schedule=None):
         self.lib = load()
         self.start = start
         if autotune:
@@ -366,6 +369,8 @@ class SplitPlan:
         self.dtype = dtype
         if arith is not None:
             self.set_arith(arith)
+        if schedule is not None:
+            self.set_schedule(schedule)
 
     def set_arith(self, arith):
         """ARITH_DF (default for complex128) or ARITH_FP64; complex64 plans are ARITH_FP32."""
@@ -374,6 +379,14 @@ class SplitPlan:
     @property
     def arith(self):
         return self.lib.dmg_split_get_arith(self.h)
+
+    def set_schedule(self, schedule):
+        """SCHEDULE_AUTO, SCHEDULE_LINES (one pass per dimension) or SCHEDULE_SPLIT (two per dimension)."""
+        check(self.lib.dmg_split_set_schedule(self.h, int(schedule)), "dmg_split_set_schedule")
+
+    @property
+    def schedule(self):
+        return self.lib.dmg_split_get_schedule(self.h)
 
     @property
     def _s(self):
@@ -453,3 +466,43 @@ class SplitPlan:
             self.free()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------- global-order I/O
+
+def io_view(decomp: "Decomp", rank: int):
+    """makeIOType's file view for one rank: (file positions, buffer offsets) of its elements in C order."""
+    import numpy as np
+    lib = load()
+    n = lib.dmg_io_view(decomp.h, int(rank), None, None, 0)
+    if n < 0:
+        raise DecompError("dmg_io_view: %s" % last_error())
+    f = np.empty(max(n, 1), dtype=np.int64)
+    m = np.empty(max(n, 1), dtype=np.int64)
+    P = ctypes.POINTER(ctypes.c_longlong)
+    lib.dmg_io_view(decomp.h, int(rank), f.ctypes.data_as(P), m.ctypes.data_as(P), n)
+    return f[:n], m[:n]
+
+
+def io_gather(decomp: "Decomp", elem_size: int, src_ptr: int, global_ptr: int, stream=None):
+    """Device to device: the array in `decomp` to global C order."""
+    check(load().dmg_io_gather(decomp.h, int(elem_size), ctypes.c_void_p(src_ptr), ctypes.c_void_p(global_ptr),
+                               ctypes.c_void_p(stream)), "dmg_io_gather")
+
+
+def io_scatter(decomp: "Decomp", elem_size: int, global_ptr: int, dst_ptr: int, stream=None):
+    """Device to device: global C order into the array in `decomp`."""
+    check(load().dmg_io_scatter(decomp.h, int(elem_size), ctypes.c_void_p(global_ptr), ctypes.c_void_p(dst_ptr),
+                                ctypes.c_void_p(stream)), "dmg_io_scatter")
+
+
+def write_file(path: str, decomp: "Decomp", elem_size: int, src_ptr: int, stream=None):
+    """Write the distributed array to `path` as the global array in C order (the reference's writeFile)."""
+    check(load().dmg_io_write_file(path.encode(), decomp.h, int(elem_size), ctypes.c_void_p(src_ptr),
+                                   ctypes.c_void_p(stream)), "dmg_io_write_file")
+
+
+def read_file(path: str, decomp: "Decomp", elem_size: int, dst_ptr: int, stream=None):
+    """Read a global C-order file into the distributed array (the reference's readFile)."""
+    check(load().dmg_io_read_file(path.encode(), decomp.h, int(elem_size), ctypes.c_void_p(dst_ptr),
+                                  ctypes.c_void_p(stream)), "dmg_io_read_file")

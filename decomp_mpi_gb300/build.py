@@ -24,6 +24,8 @@ LIB_PATH = os.path.join(PKG_DIR, LIB_NAME)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 CC = os.environ.get("CC", "gcc")
+# extra nvcc flags, e.g. "-DDMG_FFT_MINB=2" to try another register budget
+NVCC_EXTRA = os.environ.get("DMG_NVCC_FLAGS", "").split()
 
 
 def _sources():
@@ -55,7 +57,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
     """Compile every source that changed and link the library; returns its path."""
     os.makedirs(BUILD_DIR, exist_ok=True)
     host, cuda = _sources()
-    headers = glob.glob(os.path.join(INCLUDE_DIR, "*.h")) + glob.glob(os.path.join(CSRC, "*", "*.h"))
+    headers = (glob.glob(os.path.join(INCLUDE_DIR, "*.h")) + glob.glob(os.path.join(CSRC, "*", "*.h")) +
+               glob.glob(os.path.join(CSRC, "*", "*.cuh")))
     incs = ["-I" + INCLUDE_DIR, "-I" + os.path.join(CSRC, "host")]
     jobs = []
     for s in host:
@@ -67,7 +70,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         o = _obj(s)
         if force or _stale(o, [s] + headers):
             jobs.append([NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                         "--expt-relaxed-constexpr", *incs, "-c", s, "-o", o])
+                         "--expt-relaxed-constexpr", *NVCC_EXTRA, *incs, "-c", s, "-o", o])
     if jobs:
         with ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
             outs = list(ex.map(_run, jobs))

@@ -53,6 +53,8 @@ int dmg_dev_alloc(void **ptr, size_t bytes);
 void dmg_dev_free(void *ptr);
 int dmg_dev_upload(void *dst, const void *src, size_t bytes);
 void *dmg_current_stream(void);
+int dmg_copy_sync(void *dst, const void *src, size_t bytes, int to_host, void *stream);
+int dmg_stream_sync(void *stream);
 
 #ifdef __cplusplus
 }

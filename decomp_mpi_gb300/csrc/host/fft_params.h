@@ -13,6 +13,12 @@
  * A block holds a tile of n x M1 x M2 values: the transform sub-axis t and
  * two vector sub-axes v1, v2 (lines next to each other in memory), and
  * loads/stores them in the orders that make the accesses contiguous.
+ *
+ * A "line" pass transforms a whole dimension at once: the planner passes
+ * A_d = L_d, B_d = 1 for every dimension, so that sub-axis 2d is x_d.  Its
+ * output order along the transformed dimension is the split FFT's slot
+ * order: slot s holds frequency k = s / pA + pB * (s % pA) (the plan's A_d
+ * and B_d), applied when the tile is stored (forward) or loaded (inverse).
  */
 #include <stdint.h>
 
@@ -61,8 +67,22 @@ struct dmg_fft_pass {
    * than as double-float pairs; E = *scale_exp */
   int32_t in_fp64, out_fp64;
   const int32_t *scale_exp;
+  /* slot order along the transform axis on the load / store side (line
+   * passes): tile coordinate s along t is layout slot s, whose value sits at
+   * line position s / perm_a + perm_b * (s % perm_a) */
+  int32_t perm_in, perm_out, perm_a, perm_b;
+  /* the side's address is base + f0(c0) + f1(c1) + f2(c2) over the tile
+   * axes (layout not ranked and the tile axes in different dimensions): the
+   * kernel tabulates f0, f1, f2 once per tile */
+  int32_t sep_in, sep_out;
   struct dmg_fft_layout in, out;
 };
+
+/* Threads per pass block; the most values a tile may hold, and the number
+ * the planner aims at (32 KB per tile buffer) for a value of es bytes. */
+#define DMG_FFT_NT 256
+#define DMG_FFT_TILE_MAX 4096
+#define DMG_FFT_TILE_TARGET(es) ((es) == 8 ? 4096 : 2048)
 
 #ifdef __cplusplus
 extern "C" {

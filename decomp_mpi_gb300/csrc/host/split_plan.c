@@ -36,7 +36,6 @@
 #endif
 
 #define MAXPASS (2 * DMG_FFT_MAXDIM)
-#define TILE_TARGET 1024
 
 enum { LAY_START = 0, LAY_A = 1, LAY_B = 2 };
 enum { BUF_DAT = 0, BUF_WORK = 1, BUF_SCRATCH = 2 };
@@ -56,6 +55,7 @@ typedef struct {
 
 typedef struct {
   struct dmg_fft_pass p;
+  int line;                 /* a whole-dimension pass of the lines schedule */
   int in_lay, out_lay;      /* LAY_* */
   int in_buf, out_buf;      /* BUF_* */
   int64_t in_base, out_base;
@@ -70,6 +70,8 @@ struct dmg_split_impl {
   int A[DMG_FFT_MAXDIM], B[DMG_FFT_MAXDIM], L[DMG_FFT_MAXDIM];
   int grid_a[DMG_FFT_MAXDIM], grid_b[DMG_FFT_MAXDIM];
   int use_first, use_second;
+  int schedule;        /* DMG_SCHEDULE_*: as asked */
+  int lines;           /* the passes built are the lines schedule */
   long long length;    /* per-rank workspace length */
   long long ext;       /* largest extent of A and B */
   long long dat_pitch; /* per-rank pitch of dat */
@@ -195,13 +197,16 @@ static int64_t layout_addr_host(const fft_layout *l, int nd, const int *x) {
   return a;
 }
 
-static int sub_len(const struct dmg_split_impl *im, int s) { return (s & 1) ? im->B[s / 2] : im->A[s / 2]; }
+/* Sub-axis s of a pass is y (s even) or z (s odd) of dimension s/2 for the
+ * factors A, B the pass uses: the plan's for split passes, A = L, B = 1 for
+ * line passes (so that sub-axis 2d is x_d). */
+static int sub_len(const int *A, const int *B, int s) { return (s & 1) ? B[s / 2] : A[s / 2]; }
 
 /* |address step| when sub-axis s moves by one from the origin */
-static int64_t sub_step(const struct dmg_split_impl *im, const fft_layout *l, int s) {
+static int64_t sub_step(const struct dmg_split_impl *im, const fft_layout *l, const int *A, int s) {
   int x0[DMG_FFT_MAXDIM] = {0, 0, 0}, x1[DMG_FFT_MAXDIM] = {0, 0, 0};
   int d = s / 2;
-  x1[d] = (s & 1) ? im->A[d] : 1;
+  x1[d] = (s & 1) ? A[d] : 1;
   if (x1[d] >= im->L[d]) return INT64_MAX / 4;
   int64_t st = layout_addr_host(l, im->ndim, x1) - layout_addr_host(l, im->ndim, x0);
   return st < 0 ? -st : st;
@@ -257,18 +262,19 @@ static void order_by_step(const int64_t *step, int32_t *order) {
   for (int i = 0; i < 3; ++i) order[i] = idx[i];
 }
 
-/* Geometry of a pass along sub-axis t from layout li to lo. */
+/* Geometry of a pass along sub-axis t (of the factors A, B) from layout li
+ * to lo. */
 static int pass_geometry(const struct dmg_split_impl *im, struct dmg_fft_pass *p, int t, const fft_layout *li,
-                         const fft_layout *lo) {
+                         const fft_layout *lo, const int *A, const int *B) {
   memset(p, 0, sizeof(*p));
   p->ndim = im->ndim;
   for (int d = 0; d < DMG_FFT_MAXDIM; ++d) {
-    p->A[d] = d < im->ndim ? im->A[d] : 1;
-    p->B[d] = d < im->ndim ? im->B[d] : 1;
+    p->A[d] = d < im->ndim ? A[d] : 1;
+    p->B[d] = d < im->ndim ? B[d] : 1;
     p->L[d] = d < im->ndim ? im->L[d] : 1;
   }
   p->t = t;
-  p->n = sub_len(im, t);
+  p->n = sub_len(A, B, t);
   if (p->n > 4096) return dmg_error(DMG_ERR_UNSUPPORTED, "FFT factor %d exceeds 4096", p->n);
   p->nfac = factorize(p->n, p->fac);
   if (p->nfac < 0) return dmg_error(DMG_ERR_UNSUPPORTED, "FFT length %d has too many prime factors", p->n);
@@ -276,8 +282,8 @@ static int pass_geometry(const struct dmg_split_impl *im, struct dmg_fft_pass *p
   int64_t best[2] = {INT64_MAX, INT64_MAX};
   int pick[2] = {-1, -1};
   for (int s = 0; s < 2 * im->ndim; ++s) {
-    if (s == t || sub_len(im, s) <= 1) continue;
-    int64_t a = sub_step(im, li, s), b = sub_step(im, lo, s);
+    if (s == t || sub_len(A, B, s) <= 1) continue;
+    int64_t a = sub_step(im, li, A, s), b = sub_step(im, lo, A, s);
     int64_t sc = a < b ? a : b;
     if (sc < best[0]) {
       best[1] = best[0];
@@ -291,9 +297,9 @@ static int pass_geometry(const struct dmg_split_impl *im, struct dmg_fft_pass *p
   }
   p->v1 = pick[0];
   p->v2 = pick[1];
-  p->nv1 = p->v1 >= 0 ? sub_len(im, p->v1) : 1;
-  p->nv2 = p->v2 >= 0 ? sub_len(im, p->v2) : 1;
-  int room = TILE_TARGET / p->n;
+  p->nv1 = p->v1 >= 0 ? sub_len(A, B, p->v1) : 1;
+  p->nv2 = p->v2 >= 0 ? sub_len(A, B, p->v2) : 1;
+  int room = DMG_FFT_TILE_TARGET(im->esize) / p->n;
   if (room < 1) room = 1;
   p->M1 = p->nv1 < room ? p->nv1 : room;
   room /= p->M1;
@@ -304,19 +310,19 @@ static int pass_geometry(const struct dmg_split_impl *im, struct dmg_fft_pass *p
   p->nbatch = 0;
   p->ntiles = (int64_t)p->nt1 * p->nt2;
   for (int s = 2 * im->ndim - 1; s >= 0; --s) {
-    if (s == t || s == p->v1 || s == p->v2 || sub_len(im, s) <= 1) continue;
+    if (s == t || s == p->v1 || s == p->v2 || sub_len(A, B, s) <= 1) continue;
     p->bsub[p->nbatch] = s;
-    p->blen[p->nbatch] = sub_len(im, s);
+    p->blen[p->nbatch] = sub_len(A, B, s);
     p->ntiles *= p->blen[p->nbatch];
     p->nbatch++;
   }
   int64_t si[3], so[3];
-  si[0] = sub_step(im, li, t);
-  so[0] = sub_step(im, lo, t);
-  si[1] = p->v1 >= 0 ? sub_step(im, li, p->v1) : INT64_MAX - 1;
-  so[1] = p->v1 >= 0 ? sub_step(im, lo, p->v1) : INT64_MAX - 1;
-  si[2] = p->v2 >= 0 ? sub_step(im, li, p->v2) : INT64_MAX;
-  so[2] = p->v2 >= 0 ? sub_step(im, lo, p->v2) : INT64_MAX;
+  si[0] = sub_step(im, li, A, t);
+  so[0] = sub_step(im, lo, A, t);
+  si[1] = p->v1 >= 0 ? sub_step(im, li, A, p->v1) : INT64_MAX - 1;
+  so[1] = p->v1 >= 0 ? sub_step(im, lo, A, p->v1) : INT64_MAX - 1;
+  si[2] = p->v2 >= 0 ? sub_step(im, li, A, p->v2) : INT64_MAX;
+  so[2] = p->v2 >= 0 ? sub_step(im, lo, A, p->v2) : INT64_MAX;
   order_by_step(si, p->load_order);
   order_by_step(so, p->store_order);
   const int axes[3] = {t, p->v1, p->v2};
@@ -328,6 +334,12 @@ static int pass_geometry(const struct dmg_split_impl *im, struct dmg_fft_pass *p
     p->load_pos[p->load_order[i]] = i;
     p->store_pos[p->store_order[i]] = i;
   }
+  /* a side is separable over the tile when its layout is and no two tile
+   * axes share a dimension */
+  int distinct = (p->kdim[1] < 0 || p->kdim[1] != p->kdim[0]) && (p->kdim[2] < 0 || p->kdim[2] != p->kdim[0]) &&
+                 (p->kdim[2] < 0 || p->kdim[2] != p->kdim[1]);
+  p->sep_in = distinct && !li->ranked;
+  p->sep_out = distinct && !lo->ranked;
   return DMG_OK;
 }
 
@@ -519,8 +531,8 @@ static int impl_upload(struct dmg_split_impl *im) {
   return DMG_OK;
 }
 
-/* Build the forward and inverse pass lists. */
-static int build_passes(struct dmg_split_impl *im) {
+/* Forward and inverse pass lists of the split schedule. */
+static int build_passes_split(struct dmg_split_impl *im) {
   int nd = im->ndim;
   int subs[MAXPASS], stage[MAXPASS];
   int K = 0;
@@ -553,8 +565,9 @@ static int build_passes(struct dmg_split_impl *im) {
     f->out_buf = BUF_WORK;
     f->out_base = ((K - 1 - k) % 2 == 0) ? 0 : upper;
     f->in_base = k == 0 ? 0 : im->fwd[k - 1].out_base;
-    int st = pass_geometry(im, &f->p, subs[k], &im->lay[in_lay], &im->lay[out_lay]);
+    int st = pass_geometry(im, &f->p, subs[k], &im->lay[in_lay], &im->lay[out_lay], im->A, im->B);
     if (st != DMG_OK) return st;
+    f->line = 0;
     f->p.sign = -1;
     /* each stage-1 pass applies its own dimension's factor exp(-2 pi i y_d k1_d / L_d)
      * after its transform; the factor is constant along the other dimensions'
@@ -573,12 +586,14 @@ static int build_passes(struct dmg_split_impl *im) {
     b->out_buf = k == K - 1 ? BUF_DAT : BUF_WORK;
     b->in_base = k == 0 ? 0 : im->inv[k - 1].out_base;
     b->out_base = k == K - 1 ? 0 : (b->in_base == 0 ? upper : 0);
-    int st = pass_geometry(im, &b->p, f->p.t, &im->lay[b->in_lay], &im->lay[b->out_lay]);
+    int st = pass_geometry(im, &b->p, f->p.t, &im->lay[b->in_lay], &im->lay[b->out_lay], im->A, im->B);
     if (st != DMG_OK) return st;
+    b->line = 0;
     b->p.sign = +1;
     b->p.twiddle = f->p.twiddle ? 2 : 0;
   }
-  int pos = snprintf(im->desc, sizeof(im->desc), "A=[%d,%d,%d] B=[%d,%d,%d] passes=%d:", im->A[0],
+  im->lines = 0;
+  int pos = snprintf(im->desc, sizeof(im->desc), "A=[%d,%d,%d] B=[%d,%d,%d] split passes=%d:", im->A[0],
                      nd > 1 ? im->A[1] : 1, nd > 2 ? im->A[2] : 1, im->B[0], nd > 1 ? im->B[1] : 1,
                      nd > 2 ? im->B[2] : 1, K);
   for (int k = 0; k < K && pos < (int)sizeof(im->desc) - 64; ++k) {
@@ -587,6 +602,101 @@ static int build_passes(struct dmg_split_impl *im) {
                     p->n, p->v1, p->M1, p->v2, p->M2, (long long)p->ntiles, p->twiddle ? " tw" : "");
   }
   return DMG_OK;
+}
+
+/* Longest dimension the lines schedule takes: a tile of DMG_FFT_TILE_TARGET
+ * values then still holds 4 lines side by side, so that the dimensions
+ * other than the innermost are read and written in runs of 4 values. */
+static int line_max(const struct dmg_split_impl *im) { return DMG_FFT_TILE_TARGET(im->esize) / 4; }
+
+static int lines_possible(const struct dmg_split_impl *im) {
+  for (int d = 0; d < im->ndim; ++d)
+    if (im->L[d] > DMG_FFT_TILE_TARGET(im->esize)) return 0;
+  return 1;
+}
+
+/* Forward and inverse pass lists of the lines schedule. */
+static int build_passes_line(struct dmg_split_impl *im) {
+  int nd = im->ndim;
+  int dims[DMG_FFT_MAXDIM], K = 0;
+  for (int d = nd - 1; d >= 0; --d)
+    if (im->L[d] > 1) dims[K++] = d;
+  int LA[DMG_FFT_MAXDIM], LB[DMG_FFT_MAXDIM];
+  for (int d = 0; d < DMG_FFT_MAXDIM; ++d) {
+    LA[d] = d < nd ? im->L[d] : 1;
+    LB[d] = 1;
+  }
+  im->nfwd = im->ninv = K;
+  const int64_t upper = im->ext;
+  const int fin = im->use_first ? LAY_A : LAY_B;
+  for (int k = 0; k < K; ++k) {
+    pass_rec *f = &im->fwd[k];
+    const int d = dims[k];
+    f->line = 1;
+    f->in_lay = k == 0 ? LAY_START : fin;
+    f->out_lay = fin;
+    f->in_buf = k == 0 ? BUF_DAT : BUF_WORK;
+    f->out_buf = BUF_WORK;
+    f->out_base = ((K - 1 - k) % 2 == 0) ? 0 : upper;
+    f->in_base = k == 0 ? 0 : im->fwd[k - 1].out_base;
+    int st = pass_geometry(im, &f->p, 2 * d, &im->lay[f->in_lay], &im->lay[f->out_lay], LA, LB);
+    if (st != DMG_OK) return st;
+    f->p.sign = -1;
+    if (im->A[d] > 1 && im->B[d] > 1) {
+      f->p.perm_out = 1;
+      f->p.perm_a = im->A[d];
+      f->p.perm_b = im->B[d];
+    }
+  }
+  for (int k = 0; k < K; ++k) {
+    const pass_rec *f = &im->fwd[K - 1 - k];
+    pass_rec *b = &im->inv[k];
+    b->line = 1;
+    b->in_lay = f->out_lay;
+    b->out_lay = f->in_lay;
+    b->in_buf = BUF_WORK;
+    b->out_buf = k == K - 1 ? BUF_DAT : BUF_WORK;
+    b->in_base = k == 0 ? 0 : im->inv[k - 1].out_base;
+    b->out_base = k == K - 1 ? 0 : (b->in_base == 0 ? upper : 0);
+    int st = pass_geometry(im, &b->p, f->p.t, &im->lay[b->in_lay], &im->lay[b->out_lay], LA, LB);
+    if (st != DMG_OK) return st;
+    b->p.sign = +1;
+    b->p.perm_in = f->p.perm_out;
+    b->p.perm_a = f->p.perm_a;
+    b->p.perm_b = f->p.perm_b;
+  }
+  im->lines = 1;
+  int pos = snprintf(im->desc, sizeof(im->desc), "A=[%d,%d,%d] B=[%d,%d,%d] lines passes=%d:", im->A[0],
+                     nd > 1 ? im->A[1] : 1, nd > 2 ? im->A[2] : 1, im->B[0], nd > 1 ? im->B[1] : 1,
+                     nd > 2 ? im->B[2] : 1, K);
+  for (int k = 0; k < K && pos < (int)sizeof(im->desc) - 64; ++k) {
+    const struct dmg_fft_pass *p = &im->fwd[k].p;
+    pos += snprintf(im->desc + pos, sizeof(im->desc) - pos, " [d=%d n=%d v1=%d x%d v2=%d x%d tiles=%lld%s]",
+                    p->t / 2, p->n, p->v1 >= 0 ? p->v1 / 2 : -1, p->M1, p->v2 >= 0 ? p->v2 / 2 : -1, p->M2,
+                    (long long)p->ntiles, p->perm_out ? " slots" : "");
+  }
+  return DMG_OK;
+}
+
+/* Pass lists for the schedule asked for (auto: lines when every dimension
+ * is at most line_max long). */
+static int build_passes(struct dmg_split_impl *im) {
+  int use_lines;
+  if (im->schedule == DMG_SCHEDULE_LINES) {
+    if (!lines_possible(im))
+      return dmg_error(DMG_ERR_UNSUPPORTED, "lines schedule: a dimension is longer than %d",
+                       DMG_FFT_TILE_TARGET(im->esize));
+    use_lines = 1;
+  } else if (im->schedule == DMG_SCHEDULE_SPLIT) {
+    use_lines = 0;
+  } else {
+    use_lines = 1;
+    for (int d = 0; d < im->ndim; ++d)
+      if (im->L[d] > line_max(im)) use_lines = 0;
+  }
+  memset(im->fwd, 0, sizeof(im->fwd));
+  memset(im->inv, 0, sizeof(im->inv));
+  return use_lines ? build_passes_line(im) : build_passes_split(im);
 }
 
 /* kernel dtype of a plan's arithmetic */
@@ -875,6 +985,25 @@ int dmg_split_set_arith(SplitPlan plan, int arith) {
 
 int dmg_split_get_arith(SplitPlan plan) { return plan ? plan->impl->arith : -1; }
 
+int dmg_split_set_schedule(SplitPlan plan, int schedule) {
+  if (!plan) return dmg_error(DMG_ERR_ARG, "dmg_split_set_schedule: NULL plan");
+  if (schedule != DMG_SCHEDULE_AUTO && schedule != DMG_SCHEDULE_LINES && schedule != DMG_SCHEDULE_SPLIT)
+    return dmg_error(DMG_ERR_ARG, "dmg_split_set_schedule: schedule %d", schedule);
+  struct dmg_split_impl *im = plan->impl;
+  int old = im->schedule;
+  im->schedule = schedule;
+  int st = build_passes(im);
+  if (st != DMG_OK) {
+    im->schedule = old;
+    build_passes(im);
+    return st;
+  }
+  impl_free_device(im); /* passes point into the device tables: upload again */
+  return DMG_OK;
+}
+
+int dmg_split_get_schedule(SplitPlan plan) { return plan ? (plan->impl->lines ? DMG_SCHEDULE_LINES : DMG_SCHEDULE_SPLIT) : -1; }
+
 int dmg_split_launches(SplitPlan plan, int direction) {
   if (!plan) return 0;
   int k = direction == FFTW_FORWARD ? plan->impl->nfwd : plan->impl->ninv;
@@ -919,13 +1048,14 @@ int dmg_split_collect_times(SplitPlan plan) {
   int K = dmg_split_pass_times(plan, im->timed_dir, ms, MAXPASS);
   if (K < 0) return K;
   /* stage-1 passes count as FFT_1 (with the fused start->A move and the
-   * twiddle), stage-2 passes as FFT_2 (with the fused A->B move) */
+   * twiddle), stage-2 passes as FFT_2 (with the fused A->B move); passes of
+   * the lines schedule as FFT_1 */
   pass_rec *list = im->timed_dir == FFTW_FORWARD ? im->fwd : im->inv;
   double all = 0;
   for (int k = 0; k < K; ++k) {
     double sec = ms[k] * 1e-3;
     all += sec;
-    if (list[k].p.t & 1) plan->times[FFT_1] += sec;
+    if (list[k].line || (list[k].p.t & 1)) plan->times[FFT_1] += sec;
     else plan->times[FFT_2] += sec;
   }
   plan->times[ALL] += all;

@@ -1,0 +1,1107 @@
+// Batched FFT pass with fused layout change (shared by the per-arithmetic
+// translation units fft_pass_f64.cu, fft_pass_f32.cu, fft_pass_df.cu).
+//
+// One launch transforms every line along one axis and writes the result in
+// another layout.  A block owns tiles of n x M1 x M2 values, persistent over
+// the tiles, in a three-buffer pipeline: the gather copies tile i+1 from the
+// input layout into a staging buffer with asynchronous copies (cp.async, in
+// the order contiguous in the input) while tile i goes through its Stockham
+// stages between two other buffers; the scatter stores the result to the
+// output layout in the order contiguous there, optionally multiplied by a
+// split twiddle, and in the split FFT's slot order for whole-dimension
+// passes.
+//
+// Stockham stage with radix r, Lp = product of earlier radices, m = n/(Lp r):
+//   a_q = w_{Lp r}^{j q} * x[j r m + q m + k],  y[(j + s Lp) m + k] = sum_q a_q w_r^{q s}
+// (j < Lp, k < m); the result is in natural order after the last stage.
+// Lengths known at compile time (powers of two 8...2048, the 2,3,5-smooth
+// cube sides 48...480) have fixed radix schedules, index arithmetic folded
+// into shifts and multiplications, and line positions XOR-swizzled (i ^ ((i /
+// V) mod V), V values per 128 bytes) so that strided stage accesses hit
+// distinct banks; other lengths take radices 8, 4, 2, 3, 5, 7 and direct DFTs
+// of larger primes from the pass.  Roots come from the pass's L1-resident
+// global table.
+//
+// Addresses: a side whose address is separable over the tile axes keeps,
+// per tile, the part of the two vector axes in shared memory and reads the
+// transform axis's part from its table; ranked layouts are evaluated per
+// value.  Values every phase needs live in shared memory and are re-read
+// after barriers, so none holds a register through the stages.
+//
+// Three arithmetics share the code: FP64 (complex128), FP32 (complex64) and
+// double-float, where a real is an unevaluated sum hi + lo of two floats
+// (48-bit significand) so that complex128 transforms run on the FP32 pipes,
+// which GB300 has about 56 times more of than FP64.  Double-float passes keep
+// their intermediates as float pairs in HBM; the first pass converts the
+// complex128 input after scaling it by 2^-E (E from the input's largest
+// exponent, so every value fits FP32's exponent range) and the last pass
+// converts back and scales by 2^E, both with integer operations.
+// Error-free transformations used: Knuth's two-sum for addition, the FMA
+// product error for multiplication.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <type_traits>
+#include "../host/dmg_internal.h"
+#include "../host/fft_params.h"
+
+namespace {
+
+constexpr int NT = DMG_FFT_NT;
+constexpr int TILE_MAX = DMG_FFT_TILE_MAX;
+
+// ---------------------------------------------------------------- double-float reals
+
+struct df {
+  float h, l;
+};
+
+__device__ __forceinline__ df df_norm(float s, float e) {  // fast two-sum, |s| >= |e|
+  const float h = s + e;
+  return df{h, e - (h - s)};
+}
+__device__ __forceinline__ df operator+(df a, df b) {
+  const float s = a.h + b.h;
+  const float v = s - a.h;
+  float e = (a.h - (s - v)) + (b.h - v);
+  e += a.l + b.l;
+  return df_norm(s, e);
+}
+__device__ __forceinline__ df operator-(df a) { return df{-a.h, -a.l}; }
+__device__ __forceinline__ df operator-(df a, df b) { return a + (-b); }
+__device__ __forceinline__ df operator*(df a, df b) {
+  const float p = a.h * b.h;
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  return df_norm(p, e);
+}
+
+// ---------------------------------------------------------------- complex types
+
+struct dfc {
+  df x, y;
+};
+template <typename T>
+struct CT;
+template <>
+struct CT<double> {
+  using type = double2;
+};
+template <>
+struct CT<float> {
+  using type = float2;
+};
+template <>
+struct CT<df> {
+  using type = dfc;
+};
+template <typename T>
+using C2 = typename CT<T>::type;
+
+// a constant in each arithmetic: v for FP64 and FP32, (hi, lo) for double-float
+template <typename T>
+__device__ __forceinline__ T cst(double v, float hi, float lo);
+template <>
+__device__ __forceinline__ double cst<double>(double v, float, float) {
+  return v;
+}
+template <>
+__device__ __forceinline__ float cst<float>(double v, float, float) {
+  return (float)v;
+}
+template <>
+__device__ __forceinline__ df cst<df>(double, float hi, float lo) {
+  return df{hi, lo};
+}
+
+template <typename T>
+__device__ __forceinline__ C2<T> mk(T x, T y) {
+  C2<T> r;
+  r.x = x;
+  r.y = y;
+  return r;
+}
+template <typename T>
+__device__ __forceinline__ C2<T> add(C2<T> a, C2<T> b) { return mk<T>(a.x + b.x, a.y + b.y); }
+template <typename T>
+__device__ __forceinline__ C2<T> sub(C2<T> a, C2<T> b) { return mk<T>(a.x - b.x, a.y - b.y); }
+template <typename T>
+__device__ __forceinline__ C2<T> mul(C2<T> a, C2<T> b) {
+  return mk<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+#ifndef DMG_DF_FUSED
+#define DMG_DF_FUSED 1
+#endif
+#if DMG_DF_FUSED
+// a*b + c*d in double-float with one renormalisation: the two leading
+// products and their exact errors (FMA), the exact sum of the leading
+// products (two-sum), and the cross terms; the a.l*b.l terms (2^-48 of the
+// result) are dropped as in the plain product.  19 FP32 operations.
+__device__ __forceinline__ df df_dot2(df a, df b, df c, df d) {
+  const float p1 = a.h * b.h;
+  const float p2 = c.h * d.h;
+  const float e1 = fmaf(a.h, b.h, -p1);
+  const float e2 = fmaf(c.h, d.h, -p2);
+  const float s = p1 + p2;
+  const float v = s - p1;
+  float t = (p1 - (s - v)) + (p2 - v);
+  t += e1 + e2;
+  t = fmaf(a.h, b.l, t);
+  t = fmaf(a.l, b.h, t);
+  t = fmaf(c.h, d.l, t);
+  t = fmaf(c.l, d.h, t);
+  return df_norm(s, t);
+}
+template <>
+__device__ __forceinline__ dfc mul<df>(dfc a, dfc b) {
+  return dfc{df_dot2(a.x, b.x, -a.y, b.y), df_dot2(a.x, b.y, a.y, b.x)};
+}
+#endif
+
+// Sum and difference whose double-float result is left unnormalised (the
+// two-sum of the leading parts plus the trailing parts, 8 operations instead
+// of 11); used where the result only feeds further additions.  Exact FP64 and
+// FP32 arithmetic is unaffected.
+#ifndef DMG_DF_LAZY
+#define DMG_DF_LAZY 1
+#endif
+__device__ __forceinline__ df df_add_lazy(df a, df b) {
+  const float s = a.h + b.h;
+  const float v = s - a.h;
+  float e = (a.h - (s - v)) + (b.h - v);
+  e += a.l + b.l;
+  return df{s, e};
+}
+template <typename T>
+__device__ __forceinline__ C2<T> addl(C2<T> a, C2<T> b) {
+  if constexpr (std::is_same<T, df>::value && DMG_DF_LAZY) {
+    return dfc{df_add_lazy(a.x, b.x), df_add_lazy(a.y, b.y)};
+  } else {
+    return add<T>(a, b);
+  }
+}
+template <typename T>
+__device__ __forceinline__ C2<T> subl(C2<T> a, C2<T> b) {
+  if constexpr (std::is_same<T, df>::value && DMG_DF_LAZY) {
+    return dfc{df_add_lazy(a.x, -b.x), df_add_lazy(a.y, -b.y)};
+  } else {
+    return sub<T>(a, b);
+  }
+}
+template <typename T>
+__device__ __forceinline__ C2<T> scl(C2<T> a, T s) { return mk<T>(a.x * s, a.y * s); }
+template <typename T>
+__device__ __forceinline__ C2<T> conj(C2<T> a) { return mk<T>(a.x, -a.y); }
+// multiply by sign*i
+template <typename T, int SIGN>
+__device__ __forceinline__ C2<T> rot90(C2<T> a) {
+  return SIGN < 0 ? mk<T>(a.y, -a.x) : mk<T>(-a.y, a.x);
+}
+
+// mathematical constants and their double-float splits
+#define K_SQRT1_2 0.707106781186547524400844362104849039, 0.7071067690849304f, 1.2101617485882343e-08f
+#define K_SQRT3_2 0.866025403784438646763723170752936183, 0.8660253882408142f, 1.5543625053737742e-08f
+#define K_C72 0.309016994374947424102293417182819059, 0.30901700258255005f, -8.207602597565256e-09f
+#define K_C144 -0.809016994374947424102293417182819059, -0.80901700258255f, 8.207602597565256e-09f
+#define K_S72 0.951056516295153572116439333379382143, 0.9510565400123596f, -2.3717205976936384e-08f
+#define K_S144 0.587785252292473129168705954639072769, 0.5877852439880371f, 8.304436249773062e-09f
+#define K_HALF 0.5, 0.5f, 0.0f
+
+template <typename T, int SIGN>
+__device__ __forceinline__ void dft4(C2<T> &a0, C2<T> &a1, C2<T> &a2, C2<T> &a3) {
+  C2<T> t0 = addl<T>(a0, a2), t1 = subl<T>(a0, a2), t2 = addl<T>(a1, a3), t3 = rot90<T, SIGN>(subl<T>(a1, a3));
+  a0 = add<T>(t0, t2);
+  a2 = sub<T>(t0, t2);
+  a1 = add<T>(t1, t3);
+  a3 = sub<T>(t1, t3);
+}
+
+template <typename T, int SIGN>
+__device__ __forceinline__ void dft8(C2<T> *a) {
+  C2<T> e0 = a[0], e1 = a[2], e2 = a[4], e3 = a[6];
+  C2<T> o0 = a[1], o1 = a[3], o2 = a[5], o3 = a[7];
+  dft4<T, SIGN>(e0, e1, e2, e3);
+  dft4<T, SIGN>(o0, o1, o2, o3);
+  const T c = cst<T>(K_SQRT1_2);
+  // o1 *= (1 + sign i) c ; o2 *= sign i ; o3 *= (-1 + sign i) c
+  C2<T> w1 = SIGN < 0 ? mk<T>(c * (o1.x + o1.y), c * (o1.y - o1.x)) : mk<T>(c * (o1.x - o1.y), c * (o1.y + o1.x));
+  C2<T> w2 = rot90<T, SIGN>(o2);
+  C2<T> w3 = SIGN < 0 ? mk<T>(c * (o3.y - o3.x), -(c * (o3.x + o3.y))) : mk<T>(-(c * (o3.x + o3.y)), c * (o3.x - o3.y));
+  a[0] = add<T>(e0, o0);
+  a[4] = sub<T>(e0, o0);
+  a[1] = add<T>(e1, w1);
+  a[5] = sub<T>(e1, w1);
+  a[2] = add<T>(e2, w2);
+  a[6] = sub<T>(e2, w2);
+  a[3] = add<T>(e3, w3);
+  a[7] = sub<T>(e3, w3);
+}
+
+template <typename T, int SIGN>
+__device__ __forceinline__ void dft3(C2<T> *a) {
+  C2<T> s = add<T>(a[1], a[2]);
+  C2<T> d = sub<T>(a[1], a[2]);
+  const T half = cst<T>(K_HALF);
+  C2<T> m = mk<T>(a[0].x - half * s.x, a[0].y - half * s.y);
+  C2<T> r = rot90<T, SIGN>(scl<T>(d, cst<T>(K_SQRT3_2)));
+  a[0] = add<T>(a[0], s);
+  a[1] = add<T>(m, r);
+  a[2] = sub<T>(m, r);
+}
+
+template <typename T, int SIGN>
+__device__ __forceinline__ void dft5(C2<T> *a) {
+  C2<T> b1 = add<T>(a[1], a[4]), b2 = add<T>(a[2], a[3]);
+  C2<T> d1 = sub<T>(a[1], a[4]), d2 = sub<T>(a[2], a[3]);
+  const T c1 = cst<T>(K_C72), c2 = cst<T>(K_C144), s1 = cst<T>(K_S72), s2 = cst<T>(K_S144);
+  C2<T> p1 = mk<T>(a[0].x + c1 * b1.x + c2 * b2.x, a[0].y + c1 * b1.y + c2 * b2.y);
+  C2<T> p2 = mk<T>(a[0].x + c2 * b1.x + c1 * b2.x, a[0].y + c2 * b1.y + c1 * b2.y);
+  C2<T> q1 = rot90<T, SIGN>(mk<T>(s1 * d1.x + s2 * d2.x, s1 * d1.y + s2 * d2.y));
+  C2<T> q2 = rot90<T, SIGN>(mk<T>(s2 * d1.x - s1 * d2.x, s2 * d1.y - s1 * d2.y));
+  a[0] = add<T>(a[0], add<T>(b1, b2));
+  a[1] = add<T>(p1, q1);
+  a[4] = sub<T>(p1, q1);
+  a[2] = add<T>(p2, q2);
+  a[3] = sub<T>(p2, q2);
+}
+
+// ---------------------------------------------------------------- complex128 <-> double-float
+
+// x * 2^-s as a float pair with FP64 arithmetic (any x); values pushed below
+// FP64's normal range become 0
+__device__ __noinline__ df to_df_slow(double x, int s) {
+  long long b = __double_as_longlong(x);
+  const int ef = (int)((b >> 52) & 0x7FF);
+  double xs;
+  if (ef == 0) {
+    // zero or subnormal: scale by two exact power-of-two factors (the result
+    // is normal whenever the subnormal matters next to the largest value)
+    if ((b & 0x000FFFFFFFFFFFFFll) == 0 || s > 0) return df{0.0f, 0.0f};
+    const int s1 = (-s) / 2, s2 = -s - s1;
+    xs = x * __longlong_as_double((long long)(1023 + s1) << 52) * __longlong_as_double((long long)(1023 + s2) << 52);
+  } else {
+    int en = ef - s;
+    if (en <= 0) return df{0.0f, 0.0f};
+    if (en > 2046) en = 2047;  // stays inf (only when the input held inf or NaN)
+    b = (b & ~(0x7FFll << 52)) | ((long long)en << 52);
+    xs = __longlong_as_double(b);
+  }
+  const float h = __double2float_rn(xs);
+  const float l = __double2float_rn(xs - (double)h);
+  return df{h, l};
+}
+
+// (hi + lo) * 2^s as a double with FP64 arithmetic (any pair)
+__device__ __noinline__ double from_df_slow(df v, int s) {
+  const double d = (double)v.h + (double)v.l;
+  long long b = __double_as_longlong(d);
+  const int ef = (int)((b >> 52) & 0x7FF);
+  if (ef == 0 || ef == 2047) return d;  // zero (or the inf/NaN of an inf/NaN input)
+  const int en = ef + s;
+  if (en >= 1 && en <= 2046) return __longlong_as_double((b & ~(0x7FFll << 52)) | ((long long)en << 52));
+  // leaves the normal range: two exact power-of-two factors
+  const int s1 = s / 2, s2 = s - s1;
+  return d * __longlong_as_double((long long)(1023 + s1) << 52) * __longlong_as_double((long long)(1023 + s2) << 52);
+}
+
+// The same conversions with integer operations only (GB300 runs FP64 and
+// FP32<->FP64 conversions at 1/64 of its FP32 rate).  A normal double's
+// 53-bit significand m splits exactly into its 24-bit rounding mh (the
+// float hi) and the remainder r = m - mh * 2^29 (|r| <= 2^28, converted to
+// the float lo); back, hi and lo rejoin as M = mh * 2^29 + round(lo scaled),
+// renormalised by at most one bit.  Values whose pair would leave FP32's
+// normal range, zeros, subnormals, infinities and NaNs take the FP64 path.
+__device__ __forceinline__ df to_df(double x, int s) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int E = (int)((b >> 52) & 0x7FF);
+  const int fe = E - s - 896;  // float biased exponent of hi before rounding
+  if (E == 0 || E == 0x7FF || fe < 53 || fe > 253) return to_df_slow(x, s);
+  const unsigned long long m = (b & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull;
+  unsigned long long mh = (m + (1ull << 28)) >> 29;  // 24 bits, or 2^24 when rounding carried
+  const long long r = (long long)m - (long long)(mh << 29);
+  int feh = fe;
+  if (mh >> 24) {
+    mh >>= 1;
+    ++feh;
+  }
+  const unsigned sign = (unsigned)(b >> 63) << 31;
+  const float h = __uint_as_float(sign | ((unsigned)feh << 23) | ((unsigned)mh & 0x7FFFFFu));
+  // lo = r * 2^(fe - 179); fe >= 53 keeps the power of two normal
+  const float l = (float)(int)r * __uint_as_float((unsigned)(fe - 52) << 23);
+  return df{h, sign ? -l : l};
+}
+
+__device__ __forceinline__ double from_df(df v, int s) {
+  const unsigned hb = __float_as_uint(v.h);
+  const int fe = (int)((hb >> 23) & 0xFF);
+  if (fe < 52 || fe == 0xFF) return from_df_slow(v, s);
+  const long long mh = (long long)((hb & 0x7FFFFFu) | 0x800000u);
+  // lo in units of 2^(fe - 179), signed relative to hi's sign; |lo| <= ulp(hi) keeps it in range
+  const float ls = v.l * __uint_as_float((unsigned)(306 - fe) << 23);
+  if (!(fabsf(ls) < 1073741824.0f)) return from_df_slow(v, s);  // lo far outside hi's last bit
+  const int r = __float2int_rn((hb >> 31) ? -ls : ls);
+  long long M = (mh << 29) + r;
+  int E = fe + 896 + s;
+  if (M >= (1ll << 53)) {
+    M >>= 1;
+    ++E;
+  } else if (M < (1ll << 52)) {
+    M <<= 1;
+    --E;
+  }
+  if (E < 1 || E > 2046 || M < (1ll << 52) || M >= (1ll << 53)) return from_df_slow(v, s);
+  const unsigned long long bits =
+      ((unsigned long long)(hb >> 31) << 63) | ((unsigned long long)E << 52) | ((unsigned long long)M & 0x000FFFFFFFFFFFFFull);
+  return __longlong_as_double((long long)bits);
+}
+
+// ---------------------------------------------------------------- addressing
+
+__device__ __forceinline__ int64_t layout_addr(const dmg_fft_layout &L, int ndim, const int *x) {
+  if (!L.ranked) {
+    int64_t a = L.base;
+#pragma unroll
+    for (int d = 0; d < DMG_FFT_MAXDIM; ++d)
+      if (d < ndim) a += __ldg(L.tab[d] + x[d]);
+    return a;
+  }
+  int32_t R = 0;
+#pragma unroll
+  for (int d = 0; d < DMG_FFT_MAXDIM; ++d)
+    if (d < ndim) R += __ldg(L.rk[d] + x[d]);
+  int64_t a = L.base + (int64_t)R * L.pitch;
+#pragma unroll
+  for (int d = 0; d < DMG_FFT_MAXDIM; ++d)
+    if (d < ndim) a += __ldg(L.tab[d] + x[d]) * __ldg(L.rstride + (size_t)d * L.nranks + R);
+  return a;
+}
+
+// Walks e = tid, tid + NT, ... through a tile in a given order, keeping the
+// (fastest, middle, slowest) coordinates with carries instead of divisions.
+struct TileWalk {
+  int ef, em, i_f, i_m, i_s, df_, dm, ds;
+  __device__ __forceinline__ TileWalk(int tid, const int32_t *pos, int n0, int n1, int n2) {
+    ef = pos[0] == 0 ? n0 : pos[1] == 0 ? n1 : n2;
+    em = pos[0] == 1 ? n0 : pos[1] == 1 ? n1 : n2;
+    i_f = tid % ef;
+    const int rest = tid / ef;
+    i_m = rest % em;
+    i_s = rest / em;
+    df_ = NT % ef;
+    const int dr = NT / ef;
+    dm = dr % em;
+    ds = dr / em;
+  }
+  __device__ __forceinline__ void next() {
+    i_f += df_;
+    const int c1 = i_f >= ef;
+    if (c1) i_f -= ef;
+    i_m += dm + c1;
+    const int c2 = i_m >= em;
+    if (c2) i_m -= em;
+    i_s += ds + c2;
+  }
+  __device__ __forceinline__ int coord(int posk) const { return posk == 0 ? i_f : posk == 1 ? i_m : i_s; }
+};
+
+// Global coordinates x_d of the element at tile offsets (c0, c1, c2).
+__device__ __forceinline__ void element_x(const dmg_fft_pass &p, const int *yb, const int *zb, int c0, int c1, int c2,
+                                          int *x) {
+#pragma unroll
+  for (int d = 0; d < DMG_FFT_MAXDIM; ++d) {
+    int y = yb[d], z = zb[d];
+    y += (p.kdim[0] == d && !p.kisz[0]) ? c0 : 0;
+    z += (p.kdim[0] == d && p.kisz[0]) ? c0 : 0;
+    y += (p.kdim[1] == d && !p.kisz[1]) ? c1 : 0;
+    z += (p.kdim[1] == d && p.kisz[1]) ? c1 : 0;
+    y += (p.kdim[2] == d && !p.kisz[2]) ? c2 : 0;
+    z += (p.kdim[2] == d && p.kisz[2]) ? c2 : 0;
+    x[d] = y + p.A[d] * z;
+  }
+}
+
+// a root of the pass's table, conjugated for the inverse
+template <typename T, int SIGN>
+__device__ __forceinline__ C2<T> root_at(const C2<T> *roots, int i) {
+  C2<T> w;
+  if constexpr (std::is_same<T, df>::value) {
+    const float4 v = __ldg(reinterpret_cast<const float4 *>(roots) + i);
+    w.x = df{v.x, v.y};
+    w.y = df{v.z, v.w};
+  } else {
+    w = __ldg(roots + i);
+  }
+  return SIGN > 0 ? conj<T>(w) : w;
+}
+
+// Radix-r butterfly on registers (r <= 8), roots from the pass's table.
+template <typename T, int SIGN>
+__device__ __forceinline__ void butterfly(C2<T> *a, int r, const C2<T> *roots, int nr) {
+  // (roots: the pass's global table of exp(-2 pi i k / n), conjugated here for the inverse)
+  if (r == 8) {
+    dft8<T, SIGN>(a);
+  } else if (r == 4) {
+    dft4<T, SIGN>(a[0], a[1], a[2], a[3]);
+  } else if (r == 2) {
+    C2<T> t0 = add<T>(a[0], a[1]);
+    a[1] = sub<T>(a[0], a[1]);
+    a[0] = t0;
+  } else if (r == 3) {
+    dft3<T, SIGN>(a);
+  } else if (r == 5) {
+    dft5<T, SIGN>(a);
+  } else {  // 7: direct, fully unrolled so that a[] stays in registers
+    C2<T> y[8];
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+      if (s < r) {
+        C2<T> acc = a[0];
+#pragma unroll
+        for (int q = 1; q < 8; ++q)
+          if (q < r) acc = add<T>(acc, mul<T>(a[q], root_at<T, SIGN>(roots, ((q * s) % r) * nr)));
+        y[s] = acc;
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < 8; ++s)
+      if (s < r) a[s] = y[s];
+  }
+}
+
+// Radix-R butterfly for R = 2, 3, 4, 5, 8 known at compile time.
+template <typename T, int SIGN, int R>
+__device__ __forceinline__ void bfly_fixed(C2<T> *a) {
+  if constexpr (R == 8) {
+    dft8<T, SIGN>(a);
+  } else if constexpr (R == 4) {
+    dft4<T, SIGN>(a[0], a[1], a[2], a[3]);
+  } else if constexpr (R == 3) {
+    dft3<T, SIGN>(a);
+  } else if constexpr (R == 5) {
+    dft5<T, SIGN>(a);
+  } else {
+    static_assert(R == 2, "radix 2, 3, 4, 5 or 8");
+    C2<T> t0 = add<T>(a[0], a[1]);
+    a[1] = sub<T>(a[0], a[1]);
+    a[0] = t0;
+  }
+}
+
+// One Stockham stage of radix r = p.fac[f] after the first Lp points, for
+// any n (radices from the pass), from `in` to `out`.
+template <typename T, int SIGN>
+__device__ __forceinline__ void stage_runtime(const dmg_fft_pass &p, int f, int Lp, const C2<T> *in, C2<T> *out,
+                                              const C2<T> *roots, int nlines, int ld, int tid) {
+  const int n = p.n;
+  const int r = p.fac[f];
+  const int nr = n / r;
+  const int m = nr / Lp;
+  const int tstep = n / (Lp * r);  // w_{Lp r}^1 = w_n^tstep
+  const int nb = nlines * nr;
+  for (int b = tid; b < nb; b += NT) {
+    const int l = b / nr;
+    const int bb = b - l * nr;
+    const int j = bb / m;
+    const int k = bb - j * m;
+    const C2<T> *xi = in + (size_t)l * ld + j * r * m + k;
+    C2<T> *yo = out + (size_t)l * ld + j * m + k;
+    const int ostep = Lp * m;
+    if (r <= 8) {
+      C2<T> a[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        if (q < r) {
+          C2<T> v = xi[q * m];
+          if (q > 0 && j > 0) v = mul<T>(v, root_at<T, SIGN>(roots, (j * q * tstep) % n));
+          a[q] = v;
+        }
+      }
+      butterfly<T, SIGN>(a, r, roots, nr);
+#pragma unroll
+      for (int s = 0; s < 8; ++s)
+        if (s < r) yo[s * ostep] = a[s];
+    } else {
+      // direct DFT of a larger prime radix, reading shared memory
+      for (int s = 0; s < r; ++s) {
+        C2<T> acc = xi[0];
+        for (int q = 1; q < r; ++q) {
+          C2<T> v = xi[q * m];
+          if (j > 0) v = mul<T>(v, root_at<T, SIGN>(roots, (int)(((int64_t)j * q * tstep) % n)));
+          acc = add<T>(acc, mul<T>(v, root_at<T, SIGN>(roots, (int)(((int64_t)q * s % r) * nr))));
+        }
+        yo[s * ostep] = acc;
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------- stages of a length known at compile time
+
+// log2 of the values per 128 bytes: the swizzle period
+template <typename T>
+__host__ __device__ constexpr int swz_shift() {
+  return sizeof(C2<T>) == 8 ? 4 : 3;
+}
+// position of value i of an NF-point line: the low bits of i XOR the next
+// ones, when NF is a multiple of the period (else i); NF = 0: i
+template <typename T, int NF>
+__device__ __forceinline__ int swz(int i) {
+  constexpr int S = swz_shift<T>();
+  if constexpr (NF > 0 && NF % (1 << S) == 0) {
+    return i ^ ((i >> S) & ((1 << S) - 1));
+  } else {
+    return i;
+  }
+}
+
+// radix of the stage after the first LP points of NF (2, 3, 5-smooth): 8s
+// while the power-of-two part allows (16 done as 4 x 4), then 4, 2, 3, 5
+__host__ __device__ constexpr int fixed_radix(int nf, int lp) {
+  const int rem = nf / lp;
+  const int p2 = rem & -rem;
+  if (p2 >= 8) return p2 == 16 ? 4 : 8;
+  if (p2 == 4) return 4;
+  if (p2 == 2) return 2;
+  if (rem % 3 == 0) return 3;
+  if (rem % 5 == 0) return 5;
+  return rem;
+}
+
+// The Stockham stage after the first LP points of NF, from `in` to `out`.
+// roots: the pass's global table.
+template <typename T, int SIGN, int NF, int LP>
+__device__ __forceinline__ void stage_fixed(const C2<T> *in, C2<T> *out, const C2<T> *roots, int nlines, int ld,
+                                            int tid) {
+  constexpr int R = fixed_radix(NF, LP);
+  constexpr int NR = NF / R;
+  constexpr int M = NR / LP;
+  constexpr int TSTEP = NF / (LP * R);
+  const int nb = nlines * NR;
+  for (int b = tid; b < nb; b += NT) {
+    const int l = b / NR;
+    const int bb = b % NR;
+    const int j = bb / M;
+    const int k = bb % M;
+    const int lo = l * ld;
+    C2<T> a[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      C2<T> v = in[lo + swz<T, NF>(j * R * M + q * M + k)];
+      if (LP > 1 && q > 0) v = mul<T>(v, root_at<T, SIGN>(roots, j * q * TSTEP));
+      a[q] = v;
+    }
+    bfly_fixed<T, SIGN, R>(a);
+#pragma unroll
+    for (int s = 0; s < R; ++s) out[lo + swz<T, NF>((j + s * LP) * M + k)] = a[s];
+  }
+  __syncthreads();
+}
+
+// Stages from LP on: `in` to `out`, then back and forth between `out` and
+// `spare`; returns the buffer holding the result.
+template <typename T, int SIGN, int NF, int LP>
+__device__ __forceinline__ C2<T> *stages_fixed(C2<T> *in, C2<T> *out, C2<T> *spare, const C2<T> *roots, int nlines,
+                                               int ld, int tid) {
+  if constexpr (LP < NF) {
+    stage_fixed<T, SIGN, NF, LP>(in, out, roots, nlines, ld, tid);
+    return stages_fixed<T, SIGN, NF, LP * fixed_radix(NF, LP)>(out, spare, out, roots, nlines, ld, tid);
+  } else {
+    (void)out;
+    (void)spare;
+    return in;
+  }
+}
+
+// A value of the pass's input: complex128 converted to double-float (scaled
+// by 2^-s) when the double-float pass reads complex128, else as stored.
+template <typename T>
+__device__ __forceinline__ C2<T> load_elem(const void *src, int64_t a, bool fp64, int s) {
+  if constexpr (std::is_same<T, df>::value) {
+    if (fp64) {
+      const double2 d = reinterpret_cast<const double2 *>(src)[a];
+      dfc r;
+      r.x = to_df(d.x, s);
+      r.y = to_df(d.y, s);
+      return r;
+    }
+  }
+  (void)fp64;
+  (void)s;
+  return reinterpret_cast<const C2<T> *>(src)[a];
+}
+
+template <typename T>
+__device__ __forceinline__ void store_elem(void *dst, int64_t a, C2<T> v, bool fp64, int s) {
+  if constexpr (std::is_same<T, df>::value) {
+    if (fp64) {
+      double2 d;
+      d.x = from_df(v.x, s);
+      d.y = from_df(v.y, s);
+      reinterpret_cast<double2 *>(dst)[a] = d;
+      return;
+    }
+  }
+  (void)fp64;
+  (void)s;
+  reinterpret_cast<C2<T> *>(dst)[a] = v;
+}
+
+// ---------------------------------------------------------------- shared memory
+
+// Carve-up of a pass block's dynamic shared memory (host and device agree):
+// the staging buffer the gather copies the next tile into, two buffers the
+// stages go between, then small tables.  Roots are read from the pass's
+// global table (L1-resident).
+struct SmemLayout {
+  int ld;             // line pitch in values (odd)
+  size_t buf_a, buf_b; // byte offsets of the stage buffers (the staging buffer is at 0)
+  size_t contrib_off; // separable address parts: gather then scatter side, 1 + M1 + M2 int64 each
+  size_t perm_off;    // int16 slot -> line position
+  size_t total;
+};
+
+// Lengths with their own kernels: powers of two 8 ... 2048 and the 2, 3,
+// 5-smooth cube sides 48 ... 480.
+__host__ __device__ constexpr bool fixed_length(int n) {
+  return n == 8 || n == 16 || n == 32 || n == 64 || n == 128 || n == 256 || n == 512 || n == 1024 || n == 2048 ||
+         n == 48 || n == 96 || n == 120 || n == 160 || n == 192 || n == 240 || n == 320 || n == 384 || n == 480;
+}
+
+template <typename T>
+__host__ __device__ inline SmemLayout smem_layout(const dmg_fft_pass &p, bool fixed) {
+  SmemLayout s;
+  const size_t es = sizeof(C2<T>);
+  const int n = p.n;
+  s.ld = n | 1;
+  const size_t one = (size_t)p.M1 * p.M2 * s.ld * es;
+  s.buf_a = one;
+  s.buf_b = 2 * one;
+  size_t pos = (3 * one + 7) & ~(size_t)7;
+  (void)fixed;
+  s.contrib_off = pos;
+  pos += (size_t)2 * (1 + p.M1 + p.M2) * sizeof(int64_t);
+  s.perm_off = pos;
+  if (p.perm_in || p.perm_out) pos += (size_t)n * sizeof(int16_t);
+  s.total = (pos + 15) & ~(size_t)15;
+  return s;
+}
+
+template <typename T>
+__host__ __device__ inline bool use_fixed(const dmg_fft_pass &p) {
+  return fixed_length(p.n);
+}
+
+// Per-tile parts of a separable side's address: part[0] = base + the tables
+// of every dimension no tile axis covers, part[1 + c] and part[1 + M1 + c]
+// the entries of the v1 and v2 dimensions.
+__device__ __forceinline__ void sep_tile_parts(const dmg_fft_layout &L, const dmg_fft_pass &p, const int *xb,
+                                               int lim1, int lim2, int tid, int64_t *part) {
+  const int M1 = p.M1;
+  const int nc = 1 + M1 + p.M2;
+  for (int i = tid; i < nc; i += NT) {
+    if (i == 0) {
+      int64_t a = L.base;
+#pragma unroll
+      for (int d = 0; d < DMG_FFT_MAXDIM; ++d)
+        if (d < p.ndim && d != p.kdim[0] && d != p.kdim[1] && d != p.kdim[2]) a += __ldg(L.tab[d] + xb[d]);
+      part[0] = a;
+    } else {
+      const int k = i <= M1 ? 1 : 2;
+      const int c = k == 1 ? i - 1 : i - 1 - M1;
+      const int d = p.kdim[k];
+      if (d >= 0 && c < (k == 1 ? lim1 : lim2)) {
+        const int x = xb[d] + (p.kisz[k] ? p.A[d] * c : c);
+        part[i] = __ldg(L.tab[d] + x);
+      } else {
+        part[i] = 0;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------- asynchronous copies
+
+// global -> shared copy of one value that completes in the background
+// (cp.async, 16 bytes through L2 only, 8 bytes through L1)
+template <int BYTES>
+__device__ __forceinline__ void copy_async(void *smem, const void *gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  if constexpr (BYTES == 16) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+  } else {
+    static_assert(BYTES == 8, "8- or 16-byte values");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+  }
+}
+__device__ __forceinline__ void copy_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void copy_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// ---------------------------------------------------------------- the pass kernel
+
+#ifndef DMG_FFT_EPT
+#define DMG_FFT_EPT 4
+#endif
+constexpr int EPT = DMG_FFT_EPT;  // values a thread stores per scatter round
+#ifndef DMG_FFT_MINB
+#define DMG_FFT_MINB 2
+#endif
+constexpr int MINB = DMG_FFT_MINB;  // resident blocks per SM the register budget allows
+
+// A tile's place in the pass.
+struct TileState {
+  int yb[DMG_FFT_MAXDIM], zb[DMG_FFT_MAXDIM];
+  int lim1, lim2, ytw;
+};
+
+// Values every phase needs.  They live in shared memory and each phase
+// reads them after a barrier, so that none of them holds a register through
+// the FFT stages.
+struct PassConsts {
+  int ld, M1, d0, mult0, sexp, td, v1_ytd, v2_ytd, in64, out64;
+  unsigned buf_a, buf_b, contrib_off, perm_off;
+  TileState ts[2];  // the tile being transformed and the one being gathered
+};
+
+__device__ __forceinline__ void tile_state(const dmg_fft_pass &p, int64_t tile, TileState &st) {
+  int64_t t = tile;
+  const int i1 = (int)(t % p.nt1);
+  t /= p.nt1;
+  const int i2 = (int)(t % p.nt2);
+  t /= p.nt2;
+  int yb[DMG_FFT_MAXDIM] = {0, 0, 0}, zb[DMG_FFT_MAXDIM] = {0, 0, 0};
+  for (int b = 0; b < p.nbatch; ++b) {
+    const int c = (int)(t % p.blen[b]);
+    t /= p.blen[b];
+    const int s = p.bsub[b];
+    if (s & 1) zb[s >> 1] += c;
+    else yb[s >> 1] += c;
+  }
+  if (p.v1 >= 0) {
+    if (p.v1 & 1) zb[p.v1 >> 1] += i1 * p.M1;
+    else yb[p.v1 >> 1] += i1 * p.M1;
+  }
+  if (p.v2 >= 0) {
+    if (p.v2 & 1) zb[p.v2 >> 1] += i2 * p.M2;
+    else yb[p.v2 >> 1] += i2 * p.M2;
+  }
+  for (int d = 0; d < DMG_FFT_MAXDIM; ++d) {
+    st.yb[d] = yb[d];
+    st.zb[d] = zb[d];
+  }
+  st.ytw = yb[p.t >> 1];
+  st.lim1 = p.v1 >= 0 ? min(p.M1, p.nv1 - i1 * p.M1) : 1;
+  st.lim2 = p.v2 >= 0 ? min(p.M2, p.nv2 - i2 * p.M2) : 1;
+}
+
+// Start the copies of a tile into the staging buffer (raw values: a
+// complex128 input of a double-float pass is converted once it is there).
+template <typename T, int NF>
+__device__ __forceinline__ void gather_async(const dmg_fft_pass &p, const PassConsts &kc, const TileState &st,
+                                             const unsigned char *sm, const void *src, int tid) {
+  constexpr bool FIXED = NF > 0;
+  const int n = FIXED ? NF : p.n;
+  const int ld = kc.ld, M1 = kc.M1;
+  int yb[DMG_FFT_MAXDIM], zb[DMG_FFT_MAXDIM];
+#pragma unroll
+  for (int d = 0; d < DMG_FFT_MAXDIM; ++d) {
+    yb[d] = st.yb[d];
+    zb[d] = st.zb[d];
+  }
+  const int lim1 = st.lim1, lim2 = st.lim2;
+  const int total = n * lim1 * lim2;
+  const int d0 = kc.d0, mult0 = kc.mult0;
+  const int64_t *pin = reinterpret_cast<const int64_t *>(sm + kc.contrib_off);
+  const int16_t *perm = reinterpret_cast<const int16_t *>(sm + kc.perm_off);
+  const int64_t *tab0 = p.in.tab[d0] + (yb[d0] + p.A[d0] * zb[d0]);
+  const int64_t in0 = p.sep_in ? pin[0] : 0;
+  C2<T> *stg = reinterpret_cast<C2<T> *>(const_cast<unsigned char *>(sm));
+  const unsigned char *gsrc = static_cast<const unsigned char *>(src);
+  TileWalk w(tid, p.load_pos, n, lim1, lim2);
+  for (int e = tid; e < total; e += NT, w.next()) {
+    const int c0 = w.coord(p.load_pos[0]), c1 = w.coord(p.load_pos[1]), c2 = w.coord(p.load_pos[2]);
+    int64_t ad;
+    if (p.sep_in) {
+      ad = in0 + __ldg(tab0 + c0 * mult0) + pin[1 + c1] + pin[1 + M1 + c2];
+    } else {
+      int x[DMG_FFT_MAXDIM];
+      element_x(p, yb, zb, c0, c1, c2, x);
+      ad = layout_addr(p.in, p.ndim, x);
+    }
+    const int i = p.perm_in ? perm[c0] : c0;
+    const int sp = (c1 + M1 * c2) * ld + swz<T, NF>(i);
+    copy_async<sizeof(C2<T>)>(stg + sp, gsrc + ad * (int64_t)sizeof(C2<T>));
+  }
+  copy_async_commit();
+}
+
+// NF > 0: length NF with a compile-time schedule; NF == 0: any length.
+template <typename T, int SIGN, int NF>
+__global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p, const void *__restrict__ src,
+                                                            void *__restrict__ dst) {
+  constexpr bool FIXED = NF > 0;
+  extern __shared__ __align__(16) unsigned char sm[];
+  __shared__ PassConsts kc;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    const SmemLayout S = smem_layout<T>(p, FIXED);
+    kc.ld = S.ld;
+    kc.M1 = p.M1;
+    kc.buf_a = (unsigned)S.buf_a;
+    kc.buf_b = (unsigned)S.buf_b;
+    kc.contrib_off = (unsigned)S.contrib_off;
+    kc.perm_off = (unsigned)S.perm_off;
+    // the transform axis's dimension and step (separable sides)
+    kc.d0 = p.kdim[0];
+    kc.mult0 = p.kisz[0] ? p.A[p.kdim[0]] : 1;
+    // the transformed dimension and, for its twiddle, which vector axes carry its y
+    const int td = p.t >> 1;
+    kc.td = td;
+    kc.v1_ytd = p.kdim[1] == td && !p.kisz[1];
+    kc.v2_ytd = p.kdim[2] == td && !p.kisz[2];
+    kc.in64 = p.in_fp64 != 0;
+    kc.out64 = p.out_fp64 != 0;
+    // scale exponent of the double-float conversions (bias removed, inputs end below 2)
+    kc.sexp = (std::is_same<T, df>::value && (p.in_fp64 || p.out_fp64)) ? __ldg(p.scale_exp) - 1022 : 0;
+    if (blockIdx.x < p.ntiles) tile_state(p, blockIdx.x, kc.ts[0]);
+  }
+  __syncthreads();
+  {
+    const int n = FIXED ? NF : p.n;
+    if (p.perm_in || p.perm_out) {
+      int16_t *perm = reinterpret_cast<int16_t *>(sm + kc.perm_off);
+      for (int i = tid; i < n; i += NT) perm[i] = (int16_t)(i / p.perm_a + p.perm_b * (i % p.perm_a));
+    }
+    if (p.sep_in && blockIdx.x < p.ntiles) {
+      int xb[DMG_FFT_MAXDIM];
+#pragma unroll
+      for (int d = 0; d < DMG_FFT_MAXDIM; ++d) xb[d] = kc.ts[0].yb[d] + p.A[d] * kc.ts[0].zb[d];
+      sep_tile_parts(p.in, p, xb, kc.ts[0].lim1, kc.ts[0].lim2, tid, reinterpret_cast<int64_t *>(sm + kc.contrib_off));
+    }
+  }
+  __syncthreads();
+  if (blockIdx.x < p.ntiles) gather_async<T, NF>(p, kc, kc.ts[0], sm, src, tid);
+
+  int cur = 0;
+  for (int64_t tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x, cur ^= 1) {
+    const int64_t next = tile + gridDim.x;
+    // ---- the tile's values are in the staging buffer ----
+    copy_async_wait_all();
+    __syncthreads();
+    // convert a complex128 input to double-float, apply the inverse split twiddle
+    if ((std::is_same<T, df>::value && kc.in64) || p.twiddle == 2) {
+      const int n = FIXED ? NF : p.n;
+      const int ld = kc.ld, M1 = kc.M1;
+      const TileState &st = kc.ts[cur];
+      const int lim1 = st.lim1, lim2 = st.lim2;
+      const int sexp = kc.sexp;
+      const C2<T> *twt = reinterpret_cast<const C2<T> *>(p.tw[kc.td]);
+      C2<T> *stg = reinterpret_cast<C2<T> *>(sm);
+      const int total = n * M1 * p.M2;
+      for (int e = tid; e < total; e += NT) {
+        const int l = e / n, i = e - (e / n) * n;
+        const int c1 = l % M1, c2 = l / M1;
+        if (c1 >= lim1 || c2 >= lim2) continue;
+        const int sp = l * ld + swz<T, NF>(i);
+        C2<T> v;
+        if constexpr (std::is_same<T, df>::value) {
+          if (kc.in64) {
+            const double2 d = *reinterpret_cast<const double2 *>(stg + sp);
+            v.x = to_df(d.x, sexp);
+            v.y = to_df(d.y, sexp);
+          } else {
+            v = stg[sp];
+          }
+        } else {
+          v = stg[sp];
+        }
+        if (p.twiddle == 2) {
+          const int ex = (st.ytw + (kc.v1_ytd ? c1 : 0) + (kc.v2_ytd ? c2 : 0)) * i;
+          if (ex) v = mul<T>(v, conj<T>(twt[ex]));
+        }
+        stg[sp] = v;
+      }
+      __syncthreads();
+    }
+    // separable parts of the scatter side of this tile
+    if (p.sep_out) {
+      int xb[DMG_FFT_MAXDIM];
+#pragma unroll
+      for (int d = 0; d < DMG_FFT_MAXDIM; ++d) xb[d] = kc.ts[cur].yb[d] + p.A[d] * kc.ts[cur].zb[d];
+      sep_tile_parts(p.out, p, xb, kc.ts[cur].lim1, kc.ts[cur].lim2, tid,
+                     reinterpret_cast<int64_t *>(sm + kc.contrib_off) + (1 + p.M1 + p.M2));
+    }
+
+    // ---- first Stockham stage: staging buffer -> A; then the next tile's copies start ----
+    {
+      const int ld = kc.ld;
+      const int nlines = p.M1 * p.M2;
+      const C2<T> *stg = reinterpret_cast<const C2<T> *>(sm);
+      C2<T> *bufA = reinterpret_cast<C2<T> *>(sm + kc.buf_a);
+      if constexpr (FIXED) {
+        stage_fixed<T, SIGN, NF, 1>(stg, bufA, reinterpret_cast<const C2<T> *>(p.roots), nlines, ld, tid);
+      } else {
+        stage_runtime<T, SIGN>(p, 0, 1, stg, bufA, reinterpret_cast<const C2<T> *>(p.roots), nlines, ld, tid);
+      }
+    }
+    if (next < p.ntiles) {
+      if (tid == 0) tile_state(p, next, kc.ts[cur ^ 1]);
+      __syncthreads();
+      if (p.sep_in) {
+        int xb[DMG_FFT_MAXDIM];
+#pragma unroll
+        for (int d = 0; d < DMG_FFT_MAXDIM; ++d) xb[d] = kc.ts[cur ^ 1].yb[d] + p.A[d] * kc.ts[cur ^ 1].zb[d];
+        sep_tile_parts(p.in, p, xb, kc.ts[cur ^ 1].lim1, kc.ts[cur ^ 1].lim2, tid,
+                       reinterpret_cast<int64_t *>(sm + kc.contrib_off));
+        __syncthreads();
+      }
+      gather_async<T, NF>(p, kc, kc.ts[cur ^ 1], sm, src, tid);
+    }
+
+    // ---- the other stages: between A and B ----
+    const C2<T> *res;
+    {
+      const int ld = kc.ld;
+      const int nlines = p.M1 * p.M2;
+      C2<T> *bufA = reinterpret_cast<C2<T> *>(sm + kc.buf_a);
+      C2<T> *bufB = reinterpret_cast<C2<T> *>(sm + kc.buf_b);
+      if constexpr (FIXED) {
+        res = stages_fixed<T, SIGN, NF, fixed_radix(NF, 1)>(bufA, bufB, bufA, reinterpret_cast<const C2<T> *>(p.roots),
+                                                            nlines, ld, tid);
+      } else {
+        const C2<T> *groots = reinterpret_cast<const C2<T> *>(p.roots);
+        C2<T> *in = bufA, *out = bufB;
+        int Lp = p.fac[0];
+        for (int f = 1; f < p.nfac; ++f) {
+          stage_runtime<T, SIGN>(p, f, Lp, in, out, groots, nlines, ld, tid);
+          Lp *= p.fac[f];
+          C2<T> *t = in;
+          in = out;
+          out = t;
+        }
+        res = in;
+      }
+    }
+
+    // ---- scatter to the output layout: every read and address, then every store ----
+    {
+      const int n = FIXED ? NF : p.n;
+      const int ld = kc.ld, M1 = kc.M1;
+      const TileState &st = kc.ts[cur];
+      int yb[DMG_FFT_MAXDIM], zb[DMG_FFT_MAXDIM];
+#pragma unroll
+      for (int d = 0; d < DMG_FFT_MAXDIM; ++d) {
+        yb[d] = st.yb[d];
+        zb[d] = st.zb[d];
+      }
+      const int lim1 = st.lim1, lim2 = st.lim2;
+      const int total = n * lim1 * lim2;
+      const int d0 = kc.d0, mult0 = kc.mult0;
+      const int64_t *pout = reinterpret_cast<const int64_t *>(sm + kc.contrib_off) + (1 + p.M1 + p.M2);
+      const int16_t *perm = reinterpret_cast<const int16_t *>(sm + kc.perm_off);
+      const int64_t *tab0 = p.out.tab[d0] + (yb[d0] + p.A[d0] * zb[d0]);
+      const int64_t out0 = p.sep_out ? pout[0] : 0;
+      const bool out64 = kc.out64;
+      const int sexp = kc.sexp;
+      const C2<T> *twt = reinterpret_cast<const C2<T> *>(p.tw[kc.td]);
+      TileWalk w(tid, p.store_pos, n, lim1, lim2);
+      for (int e0 = 0; e0 < total; e0 += NT * EPT) {
+        int64_t ad[EPT];
+        C2<T> v[EPT];
+        bool ok[EPT];
+#pragma unroll
+        for (int u = 0; u < EPT; ++u) {
+          ok[u] = e0 + tid + u * NT < total;
+          if (ok[u]) {
+            const int c0 = w.coord(p.store_pos[0]), c1 = w.coord(p.store_pos[1]), c2 = w.coord(p.store_pos[2]);
+            const int i = p.perm_out ? perm[c0] : c0;
+            C2<T> x = res[(c1 + M1 * c2) * ld + swz<T, NF>(i)];
+            if (p.twiddle == 1) {
+              const int ex = (st.ytw + (kc.v1_ytd ? c1 : 0) + (kc.v2_ytd ? c2 : 0)) * c0;
+              if (ex) x = mul<T>(x, twt[ex]);
+            }
+            v[u] = x;
+            if (p.sep_out) {
+              ad[u] = out0 + __ldg(tab0 + c0 * mult0) + pout[1 + c1] + pout[1 + M1 + c2];
+            } else {
+              int xg[DMG_FFT_MAXDIM];
+              element_x(p, yb, zb, c0, c1, c2, xg);
+              ad[u] = layout_addr(p.out, p.ndim, xg);
+            }
+          }
+          w.next();
+        }
+#pragma unroll
+        for (int u = 0; u < EPT; ++u)
+          if (ok[u]) store_elem<T>(dst, ad[u], v[u], out64, sexp);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T, int SIGN, int NF>
+int launch_k(const dmg_fft_pass &p, const void *src, void *dst, cudaStream_t s) {
+  const size_t smem = smem_layout<T>(p, NF > 0).total;
+  auto k = fft_pass_kernel<T, SIGN, NF>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return dmg_error(DMG_ERR_CUDA, "fft pass smem %zu: %s", smem, cudaGetErrorString(e));
+  }
+  int dev = 0, nsm = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, NT, smem);
+  if (per_sm < 1) return dmg_error(DMG_ERR_UNSUPPORTED, "fft pass does not fit on an SM (smem %zu)", smem);
+  int64_t grid = (int64_t)nsm * per_sm;
+  if (grid > p.ntiles) grid = p.ntiles;
+  if (grid < 1) return DMG_OK;
+  k<<<(unsigned)grid, NT, smem, s>>>(p, src, dst);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return dmg_error(DMG_ERR_CUDA, "fft pass launch: %s", cudaGetErrorString(e));
+  return DMG_OK;
+}
+
+template <typename T, int SIGN>
+int launch_sign(const dmg_fft_pass &p, const void *src, void *dst, cudaStream_t s) {
+  switch (p.n) {
+    case 8: return launch_k<T, SIGN, 8>(p, src, dst, s);
+    case 16: return launch_k<T, SIGN, 16>(p, src, dst, s);
+    case 32: return launch_k<T, SIGN, 32>(p, src, dst, s);
+    case 64: return launch_k<T, SIGN, 64>(p, src, dst, s);
+    case 128: return launch_k<T, SIGN, 128>(p, src, dst, s);
+    case 256: return launch_k<T, SIGN, 256>(p, src, dst, s);
+    case 512: return launch_k<T, SIGN, 512>(p, src, dst, s);
+    case 1024: return launch_k<T, SIGN, 1024>(p, src, dst, s);
+    case 2048: return launch_k<T, SIGN, 2048>(p, src, dst, s);
+    case 48: return launch_k<T, SIGN, 48>(p, src, dst, s);
+    case 96: return launch_k<T, SIGN, 96>(p, src, dst, s);
+    case 120: return launch_k<T, SIGN, 120>(p, src, dst, s);
+    case 160: return launch_k<T, SIGN, 160>(p, src, dst, s);
+    case 192: return launch_k<T, SIGN, 192>(p, src, dst, s);
+    case 240: return launch_k<T, SIGN, 240>(p, src, dst, s);
+    case 320: return launch_k<T, SIGN, 320>(p, src, dst, s);
+    case 384: return launch_k<T, SIGN, 384>(p, src, dst, s);
+    case 480: return launch_k<T, SIGN, 480>(p, src, dst, s);
+    default: return launch_k<T, SIGN, 0>(p, src, dst, s);
+  }
+}
+
+// Launch one pass in arithmetic T (checked by the caller).
+template <typename T>
+int launch_pass(const dmg_fft_pass &p, const void *src, void *dst, void *stream) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // the gather copies whole values asynchronously: both arrays need their natural alignment
+  if ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) % sizeof(C2<T>) != 0)
+    return dmg_error(DMG_ERR_ARG, "fft pass: buffers must be aligned to %zu bytes", sizeof(C2<T>));
+  return p.sign < 0 ? launch_sign<T, -1>(p, src, dst, s) : launch_sign<T, 1>(p, src, dst, s);
+}
+
+template <typename T>
+size_t pass_smem(const dmg_fft_pass &p) {
+  return smem_layout<T>(p, use_fixed<T>(p)).total;
+}
+
+}  // namespace

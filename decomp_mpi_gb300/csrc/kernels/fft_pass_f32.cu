@@ -1,0 +1,8 @@
+// FFT pass kernels in one arithmetic (float); see fft_pass.cuh.
+#include "fft_pass.cuh"
+
+size_t dmg_fft_pass_smem_f32(const dmg_fft_pass *p) { return pass_smem<float>(*p); }
+
+int dmg_fft_pass_launch_f32(const dmg_fft_pass *p, const void *src, void *dst, void *stream) {
+  return launch_pass<float>(*p, src, dst, stream);
+}

@@ -34,6 +34,21 @@ extern "C" int dmg_dev_upload(void *dst, const void *src, size_t bytes) {
   return DMG_OK;
 }
 
+// Copy between host and device on a stream and wait for it (file I/O paths).
+extern "C" int dmg_copy_sync(void *dst, const void *src, size_t bytes, int to_host, void *stream) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemcpyAsync(dst, src, bytes, to_host ? cudaMemcpyDeviceToHost : cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return dmg_error(DMG_ERR_CUDA, "copy of %zu bytes: %s", bytes, cudaGetErrorString(e));
+  return DMG_OK;
+}
+
+extern "C" int dmg_stream_sync(void *stream) {
+  cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return dmg_error(DMG_ERR_CUDA, "cudaStreamSynchronize: %s", cudaGetErrorString(e));
+  return DMG_OK;
+}
+
 // CUDA-event pairs used by plan timing and the autotuner.
 struct dmg_events {
   int count;

@@ -143,6 +143,20 @@ SplitPlan dmg_makeParallelPlanTyped(Decomp start, int *initial_factor, void *dat
  * complex128; complex64 plans accept only DMG_ARITH_FP32). */
 int dmg_split_set_arith(SplitPlan plan, int arith);
 int dmg_split_get_arith(SplitPlan plan);
+/* Pass schedule.  Both give the reference's output in the same workspace
+ * slots.  LINES: one pass per dimension transforms all L_d points at once
+ * and stores them in slot order (one HBM round trip per dimension; needs
+ * L_d <= 2048 for complex128, 4096 for complex64).  SPLIT: the reference's
+ * two stages, a pass per factor of each dimension with the twiddle between.
+ * AUTO (default): LINES when every L_d is at most 512 (complex128) or 1024
+ * (complex64), else SPLIT. */
+#define DMG_SCHEDULE_AUTO 0
+#define DMG_SCHEDULE_LINES 1
+#define DMG_SCHEDULE_SPLIT 2
+/** Select the pass schedule (no counterpart in the reference). */
+int dmg_split_set_schedule(SplitPlan plan, int schedule);
+/** The schedule in use: DMG_SCHEDULE_LINES or DMG_SCHEDULE_SPLIT. */
+int dmg_split_get_schedule(SplitPlan plan);
 /** Status-returning run on an explicit stream (NULL = legacy default). */
 int dmg_split_run(SplitPlan plan, int direction, void *stream);
 /** Rebind the device buffers of a plan (same sizes). */

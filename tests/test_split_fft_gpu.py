@@ -25,7 +25,7 @@ class Run:
     """One split plan on the GPU with its buffers."""
 
     def __init__(self, P, spec, shape, cuda, mode=0, B=None, dtype=api.C128, work_len=None, seed=0, arith=None,
-                 scale=1.0):
+                 scale=1.0, schedule=None):
         import torch
         self.torch = torch
         self.P, self.spec, self.shape = P, spec, tuple(shape)
@@ -42,7 +42,7 @@ class Run:
         self.work = torch.zeros(P * self.wl, dtype=tdt, device=cuda)
         self.plan = api.SplitPlan(self.S, self.dat.data_ptr(), self.wl, self.work.data_ptr(),
                                   slab=mode if mode < 2 else 0, B=B if mode == 2 else None, dtype=dtype,
-                                  arith=arith)
+                                  arith=arith, schedule=schedule)
         self.mode, self.B = mode, B
         self.stream = torch.cuda.current_stream(cuda).cuda_stream
 
@@ -93,9 +93,12 @@ CASES = [
 ]
 
 
+@pytest.mark.parametrize("schedule", [api.SCHEDULE_LINES, api.SCHEDULE_SPLIT], ids=["lines", "split"])
 @pytest.mark.parametrize("P,spec,shape,mode,B", CASES, ids=[str(c[2]) + "m%d" % c[3] for c in CASES])
-def test_forward_and_inverse_fp64(P, spec, shape, mode, B, cuda):
-    r = Run(P, spec, shape, cuda, mode, B)
+def test_forward_and_inverse_fp64(P, spec, shape, mode, B, schedule, cuda):
+    """Double-float arithmetic (the complex128 default) in both pass schedules."""
+    r = Run(P, spec, shape, cuda, mode, B, schedule=schedule)
+    assert r.plan.schedule == schedule
     got = r.forward()
     exp, mask = O.split_expected_output(P, spec, r.glob, r.wl, mode, B)
     assert _rel(got[mask], exp[mask]) < TOL_C128
@@ -104,12 +107,14 @@ def test_forward_and_inverse_fp64(P, spec, shape, mode, B, cuda):
     assert _rel(g, r.glob) < TOL_C128
 
 
+@pytest.mark.parametrize("schedule", [api.SCHEDULE_LINES, api.SCHEDULE_SPLIT], ids=["lines", "split"])
 @pytest.mark.parametrize("P,spec,shape", [
     (4, "packed:block(64,2)|block(64,2)|local(64)", (64, 64, 64)),
     (16, "packed:block(120,4)|block(120,4)|local(120)", (120, 120, 120)),
+    (64, "packed:frev(16,8,block(128,8))|rotate(3,block(64,8))|local(32)", (128, 64, 32)),
 ])
-def test_forward_and_inverse_fp32(P, spec, shape, cuda):
-    r = Run(P, spec, shape, cuda, dtype=api.C64)
+def test_forward_and_inverse_fp32(P, spec, shape, schedule, cuda):
+    r = Run(P, spec, shape, cuda, dtype=api.C64, schedule=schedule)
     got = r.forward()
     exp, mask = O.split_expected_output(P, spec, r.glob, r.wl)
     assert _rel(got[mask].astype(np.complex128), exp[mask]) < TOL_C64
@@ -146,11 +151,12 @@ def test_linear_index_pattern_roundtrip(cuda):
     assert np.max(np.abs(g - glob)) < 1e-9
 
 
+@pytest.mark.parametrize("schedule", [api.SCHEDULE_LINES, api.SCHEDULE_SPLIT], ids=["lines", "split"])
 @pytest.mark.parametrize("P,spec,shape,mode,B", [CASES[0], CASES[2], CASES[4], CASES[6], CASES[8], CASES[10]],
                          ids=["64c", "48c", "14x21x11", "allA1", "1d", "frev128"])
-def test_forward_and_inverse_native_fp64(P, spec, shape, mode, B, cuda):
+def test_forward_and_inverse_native_fp64(P, spec, shape, mode, B, schedule, cuda):
     """The same transforms in native FP64 arithmetic (DMG_ARITH_FP64)."""
-    r = Run(P, spec, shape, cuda, mode, B, arith=api.ARITH_FP64)
+    r = Run(P, spec, shape, cuda, mode, B, arith=api.ARITH_FP64, schedule=schedule)
     assert r.plan.arith == api.ARITH_FP64
     got = r.forward()
     exp, mask = O.split_expected_output(P, spec, r.glob, r.wl, mode, B)
@@ -187,3 +193,37 @@ def test_double_float_zero_input(cuda):
     assert not np.any(got)
     assert r.plan.arith == api.ARITH_DF
     del torch
+
+
+@pytest.mark.parametrize("dtype", [api.C128, api.C64], ids=["c128", "c64"])
+def test_long_dimension_schedules(dtype, cuda):
+    """1024-point dimensions: auto picks the split schedule for complex128 and lines for complex64; both
+    schedules give the same slots."""
+    P, spec, shape = 4, "packed:block(1024,2)|block(48,2)", (1024, 48)
+    tol = TOL_C128 if dtype == api.C128 else TOL_C64
+    r = Run(P, spec, shape, cuda, dtype=dtype)
+    assert r.plan.schedule == (api.SCHEDULE_SPLIT if dtype == api.C128 else api.SCHEDULE_LINES)
+    for sched in (api.SCHEDULE_LINES, api.SCHEDULE_SPLIT):
+        r.plan.set_schedule(sched)
+        got = r.forward().astype(np.complex128)
+        exp, mask = O.split_expected_output(P, spec, r.glob, r.wl)
+        assert _rel(got[mask], exp[mask]) < tol
+        back = r.inverse().astype(np.complex128)
+        g = O.gather_global(P, spec, back, r.dp, r.shape) / np.prod(r.shape)
+        assert _rel(g, r.glob) < tol
+        r.dat /= float(np.prod(r.shape))  # the unnormalised inverse left N times the input
+
+
+def test_schedule_rejects_too_long_lines(cuda):
+    """A dimension longer than a tile cannot run as one line pass."""
+    import torch
+    P, spec = 4, "packed:block(4096,2)|block(8,2)"
+    comm = api.Comm(P)
+    S = api.decomp_from_spec(comm, spec)
+    work = torch.zeros(P * 4 * S.extent(), dtype=torch.complex128, device=cuda)
+    dat = torch.zeros(P * S.extent(), dtype=torch.complex128, device=cuda)
+    plan = api.SplitPlan(S, dat.data_ptr(), 4 * S.extent(), work.data_ptr())
+    assert plan.schedule == api.SCHEDULE_SPLIT
+    with pytest.raises(RuntimeError):
+        plan.set_schedule(api.SCHEDULE_LINES)
+    assert plan.schedule == api.SCHEDULE_SPLIT
