@@ -484,6 +484,233 @@ def run_sweep(args):
                         back.free()
 
 
+
+SERVE_SIDES = [48, 64, 96, 120, 128, 160, 192, 240, 256, 320, 384, 480, 512]
+
+
+def run_serve(args):
+    """Served form: a Poisson stream (2000 req/s, seed 3) of block->rotate + split FFT forward + inverse jobs on
+    a 4x4 virtual grid, sides from SERVE_SIDES, complex64 or complex128 with p = 1/2.  Runs the stream on the
+    server (stream slots, admission by free HBM, same-shape batching), then the same jobs one at a time on a
+    one-slot server without batching ("alone"), and reports both."""
+    import numpy as np
+    import torch
+
+    from decomp_mpi_gb300 import api
+
+    grid, P = 4, 16
+    rng = np.random.default_rng(3)
+    njobs = args.jobs
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, njobs))
+    sides = rng.choice(SERVE_SIDES if not args.quick else SERVE_SIDES[:7], njobs)
+    dtypes = np.where(rng.random(njobs) < 0.5, api.C128, api.C64)
+    classes = sorted(set(zip(sides.tolist(), dtypes.tolist())))
+    flops = float(sum(2 * flops_per_transform(int(sd) ** 3) for sd in sides))
+
+    def make_server(slots, batch):
+        return api.Server(grid, args.arena_gb << 30, slots=slots, max_batch=batch)
+
+    srv = make_server(args.slots, args.batch)
+    # one input per class (uniform[-1,1)), pinned spectrum / output arrays per class: jobs of a class carry
+    # the same values, so concurrent jobs of a class write identical results into them
+    bufs = {}
+    for side, dt in classes:
+        blk, rot = api.cube_specs(side, grid)
+        n_in, n_spec, n_out = srv.sizes(side, dt)
+        tdt = torch.complex128 if dt == api.C128 else torch.complex64
+        g = torch.Generator().manual_seed(side * 7 + dt)
+        x = torch.empty(n_in, dtype=tdt)
+        x.real.uniform_(-1, 1, generator=g)
+        x.imag.uniform_(-1, 1, generator=g)
+        bufs[(side, dt)] = (x.pin_memory(), torch.zeros(n_spec, dtype=tdt).pin_memory(),
+                            torch.zeros(n_out, dtype=tdt).pin_memory())
+    # warm-up: each class once (plans, device tables)
+    for c in classes:
+        hi, hs, ho = bufs[c]
+        srv.submit(c[0], c[1], hi.data_ptr(), hs.data_ptr(), ho.data_ptr())
+    srv.drain()
+    srv.poll()
+
+    def stream_run(server, paced):
+        t0 = time.monotonic()
+        ids = {}
+        for i in range(njobs):
+            if paced:
+                wait = t0 + arrivals[i] - time.monotonic()
+                if wait > 0:
+                    time.sleep(wait)
+            c = (int(sides[i]), int(dtypes[i]))
+            hi, hs, ho = bufs[c]
+            ids[server.submit(c[0], c[1], hi.data_ptr(), hs.data_ptr(), ho.data_ptr())] = i
+            if not paced:
+                server.drain()
+        server.drain()
+        t1 = time.monotonic()
+        done = server.poll()
+        assert len(done) == njobs and all(d["status"] == 0 for d in done), "failed jobs"
+        return done, t1 - t0, ids
+
+    done, span, ids = stream_run(srv, paced=True)
+    srv.close()
+    lat = np.array([d["t_done"] - d["t_submit"] for d in done])
+    batches = np.array([d["batch"] for d in done])
+
+    # alone: one slot, no batching, each job run by itself; latency as if the same arrivals queued for it
+    alone = make_server(1, 1)
+    for c in classes:
+        hi, hs, ho = bufs[c]
+        alone.submit(c[0], c[1], hi.data_ptr(), hs.data_ptr(), ho.data_ptr())
+    alone.drain()
+    alone.poll()
+    adone, aspan, aids = stream_run(alone, paced=False)
+    alone.close()
+    service = np.zeros(njobs)
+    for d in adone:
+        service[aids[d["id"]]] = d["t_done"] - d["t_start"]
+    finish, qlat = 0.0, np.zeros(njobs)
+    for i in range(njobs):
+        finish = max(arrivals[i], finish) + service[i]
+        qlat[i] = finish - arrivals[i]
+
+    # accuracy of the round trip per class (the inverse holds N times the rotated input)
+    errs = {}
+    for side, dt in classes:
+        if side > 128:
+            continue  # the host check gathers the cube: small classes only
+        blk, rot = api.cube_specs(side, grid)
+        comm = api.Comm(P)
+        pb = api.decomp_from_spec(comm, blk).extent()
+        pr = api.decomp_from_spec(comm, rot).extent()
+        from oracle import oracle as O  # the checker only
+        hi, hs, ho = bufs[(side, dt)]
+        gin = O.gather_global(P, blk, hi.numpy().astype(np.complex128), pb, (side,) * 3)
+        gout = O.gather_global(P, rot, ho.numpy().astype(np.complex128), pr, (side,) * 3) / side ** 3
+        errs["%d%s" % (side, "c128" if dt == api.C128 else "c64")] = float(
+            np.linalg.norm(gout - gin) / np.linalg.norm(gin))
+    line = {
+        "metric": "served split 3D FFT jobs (forward + inverse): throughput and latency",
+        "jobs": njobs, "offered_rate_per_s": args.rate, "arrival_span_s": round(float(arrivals[-1]), 4),
+        "served": {"makespan_s": round(span, 4), "jobs_per_s": round(njobs / span, 2),
+                   "gflops": round(flops / span / 1e9, 2), "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 3),
+                   "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 3),
+                   "mean_batch": round(float(batches.mean()), 2), "max_batch": int(batches.max()),
+                   "slots": args.slots, "max_batch_limit": args.batch, "arena_gib": args.arena_gb},
+        "alone": {"busy_s": round(float(service.sum()), 4), "jobs_per_s": round(njobs / float(service.sum()), 2),
+                  "gflops": round(flops / float(service.sum()) / 1e9, 2),
+                  "p50_ms_same_arrivals": round(1e3 * float(np.percentile(qlat, 50)), 3),
+                  "p99_ms_same_arrivals": round(1e3 * float(np.percentile(qlat, 99)), 3)},
+        "roundtrip_rel_l2": errs,
+        "config": {"grid": "4x4 virtual", "sides": SERVE_SIDES if not args.quick else SERVE_SIDES[:7],
+                   "dtypes": "complex64 / complex128, p = 1/2", "seed": 3,
+                   "chain": "H2D, block->rotate reshape, split FFT forward, spectrum D2H, inverse, output D2H"},
+    }
+    print(json.dumps(line))
+
+
+def run_precision(args):
+    """Precision form: 1024^3 complex64, complex Gaussian N(0,1) (seed 2) plus 16 unit-amplitude plane waves at
+    random wavenumbers (seed 2), on an 8x8 grid in the block decomposition.  Split 3D FFT forward in FP32; the
+    FP64-accuracy reference is the double-float complex128 transform of the same values on the GPU (pinned
+    against numpy's FP64 FFT to 1e-14 at smaller sizes); native FP64 is timed beside it."""
+    import numpy as np
+    import torch
+
+    from decomp_mpi_gb300 import api
+
+    n = args.n if args.n != N_SIDE else 1024
+    g = 8
+    Pp = g * g
+    dev = torch.device("cuda:0")
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    comm = api.Comm(Pp)
+    spec = "packed:block(%d,%d)|block(%d,%d)|local(%d)" % (n, g, n, g, n)
+    D = api.decomp_from_spec(comm, spec)
+    pitch = D.extent()
+    N = n ** 3
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(2)
+    glob = torch.empty(N, dtype=torch.complex64, device=dev)
+    glob.real.normal_(0, math.sqrt(0.5), generator=gen)
+    glob.imag.normal_(0, math.sqrt(0.5), generator=gen)
+    rng = np.random.default_rng(2)
+    waves = rng.integers(0, n, size=(16, 3))
+    idx = torch.arange(n, device=dev, dtype=torch.float64)
+    g3 = glob.view(n, n, n)
+    for k in waves:
+        e = [torch.exp(2j * math.pi * float(k[d]) * idx / n) for d in range(3)]
+        g3 += (e[0][:, None, None] * e[1][None, :, None] * e[2][None, None, :]).to(torch.complex64)
+    x64 = torch.empty(Pp * pitch, dtype=torch.complex64, device=dev)
+    api.io_scatter(D, 8, glob.data_ptr(), x64.data_ptr(), sh)
+    del g3, glob
+    x128 = x64.to(torch.complex128)
+    probe = api.SplitPlan(D, 1 << 20, 1 << 40, 1 << 21, dtype=api.C64)
+    ext = probe.extent64
+    probe.free()
+    length = 2 * ext
+    w64 = torch.empty(Pp * length, dtype=torch.complex64, device=dev)
+    sp64 = api.SplitPlan(D, x64.data_ptr(), length, w64.data_ptr(), dtype=api.C64)
+
+    def timed(plan, reps=3):
+        plan.run(api.FFTW_FORWARD, sh)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ms = []
+        for _ in range(reps):
+            e0.record(stream)
+            plan.run(api.FFTW_FORWARD, sh)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return statistics.median(ms)
+
+    ms32 = timed(sp64)
+    B = sp64.decomp_B()
+    spec32 = w64.view(Pp, length)[:, :ext].contiguous()
+    out32 = torch.empty(N, dtype=torch.complex64, device=dev)
+    api.io_gather(B, 8, spec32.data_ptr(), out32.data_ptr(), sh)
+    del spec32, w64
+    sp64.free()
+    del x64
+    w128 = torch.empty(Pp * length, dtype=torch.complex128, device=dev)
+    sp128 = api.SplitPlan(D, x128.data_ptr(), length, w128.data_ptr(), dtype=api.C128)
+    ms_df = timed(sp128)
+    spec128 = w128.view(Pp, length)[:, :ext].contiguous()
+    ref = torch.empty(N, dtype=torch.complex128, device=dev)
+    api.io_gather(sp128.decomp_B(), 16, spec128.data_ptr(), ref.data_ptr(), sh)
+    del spec128
+    sp128.set_arith(api.ARITH_FP64)
+    ms_fp64 = timed(sp128, reps=2)
+    torch.cuda.synchronize()
+    diff = out32.to(torch.complex128) - ref
+    rel_l2 = float((torch.linalg.vector_norm(diff) / torch.linalg.vector_norm(ref)).item())
+    max_abs = float(diff.abs().max().item())
+    max_ref = float(ref.abs().max().item())
+    # planted peaks: frequency k sits in slot s = k / B + A (k % B) of each dimension (the plan's factors)
+    A, Bf = sp128.A_factors, [n // a for a in sp128.A_factors]
+    peaks32, peaks64 = [], []
+    for k in waves:
+        s = [int(k[d]) // Bf[d] + A[d] * (int(k[d]) % Bf[d]) for d in range(3)]
+        lin = (s[0] * n + s[1]) * n + s[2]
+        peaks32.append(abs(complex(out32[lin].item()) - N) / N)
+        peaks64.append(abs(complex(ref[lin].item()) - N) / N)
+    flops = flops_per_transform(N)
+    line = {
+        "metric": "precision form: split 3D FFT of 1024^3 complex64, error against an FP64-accuracy transform",
+        "config": {"n": n, "grid": "8x8 virtual", "input": "complex N(0,1), seed 2, + 16 unit plane waves (seed 2)",
+                   "schedule": "lines" if sp128.schedule == api.SCHEDULE_LINES else "split"},
+        "fp32": {"ms": round(ms32, 3), "gflops": round(flops / (ms32 * 1e-3) / 1e9, 1),
+                 "hbm_gbs": round(6 * N * 8 / (ms32 * 1e-3) / 1e9, 1),
+                 "hbm_note": "three passes, each reading and writing the array once (6 N * 8 bytes)"},
+        "double_float_c128": {"ms": round(ms_df, 3), "gflops": round(flops / (ms_df * 1e-3) / 1e9, 1)},
+        "native_fp64_c128": {"ms": round(ms_fp64, 3), "gflops": round(flops / (ms_fp64 * 1e-3) / 1e9, 1)},
+        "fp32_error": {"rel_l2": rel_l2, "max_abs": max_abs, "max_abs_over_max": max_abs / max_ref,
+                       "planted_peak_rel_dev_max": max(peaks32), "reference_peak_rel_dev_max": max(peaks64)},
+        "tensor_cores": "not used: the FP32 passes are bound by instruction issue and HBM, not FMA throughput",
+    }
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--sweep", action="store_true", help="reshape bandwidth sweep (one JSON line per case)")
@@ -493,6 +720,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=N_SIDE, help="cube side (the headline workload is 512)")
+    ap.add_argument("--serve", action="store_true", help="served form: Poisson stream of mixed-size jobs")
+    ap.add_argument("--precision", action="store_true", help="precision form: 1024^3 complex64 with error")
+    ap.add_argument("--jobs", type=int, default=200, help="with --serve: jobs in the stream")
+    ap.add_argument("--rate", type=float, default=2000.0, help="with --serve: mean arrivals per second")
+    ap.add_argument("--slots", type=int, default=4, help="with --serve: stream slots")
+    ap.add_argument("--batch", type=int, default=8, help="with --serve: jobs that may share launches")
+    ap.add_argument("--arena-gb", dest="arena_gb", type=int, default=96, help="with --serve: device arena")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -502,6 +736,12 @@ def main():
         return  # one GPU per run in this build: extra ranks do no work
     if args.sweep:
         run_sweep(args)
+        return
+    if args.serve:
+        run_serve(args)
+        return
+    if args.precision:
+        run_precision(args)
         return
     run_gpu(args)
 

@@ -108,6 +108,16 @@ SIGNATURES = {
     "dmg_split_set_arith": (_i, [_vp, _i]),
     "dmg_split_get_arith": (_i, [_vp]),
     "dmg_split_set_schedule": (_i, [_vp, _i]),
+    "dmg_split_run_batch": (_i, [_vp, _i, _vp, _i, _vp, _vp, _vp]),
+    "dmg_split_batch_launches": (_i, [_vp, _i, _i]),
+    "dmg_split_extent64": (_ll, [_vp]),
+    "dmg_server_create": (_vp, [_i, _ll, _i, _i]),
+    "dmg_server_job_sizes": (_i, [_vp, _i, _i, ctypes.POINTER(_ll), ctypes.POINTER(_ll), ctypes.POINTER(_ll)]),
+    "dmg_server_submit": (_ll, [_vp, _vp]),
+    "dmg_server_poll": (_i, [_vp, _vp, _i]),
+    "dmg_server_drain": (_i, [_vp]),
+    "dmg_server_status": (_i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_ll)]),
+    "dmg_server_destroy": (None, [_vp]),
     "dmg_makeGlobalDecomp": (_vp, [_vp, _i, _ip]),
     "dmg_io_gather": (_i, [_vp, _i, _vp, _vp, _vp]),
     "dmg_io_scatter": (_i, [_vp, _i, _vp, _vp, _vp]),

@@ -380,6 +380,20 @@ class SplitPlan:
     def arith(self):
         return self.lib.dmg_split_get_arith(self.h)
 
+    def run_batch(self, direction, dats, works, scales=None, stream=None):
+        """dmg_split_run_batch: one run over several (dat, work) device arrays; scales: device int pointers
+        (needed for double-float plans)."""
+        n = len(dats)
+        D = (ctypes.c_void_p * n)(*[ctypes.c_void_p(x) for x in dats])
+        W = (ctypes.c_void_p * n)(*[ctypes.c_void_p(x) for x in works])
+        S = (ctypes.c_void_p * n)(*[ctypes.c_void_p(x) for x in (scales or [0] * n)])
+        check(self.lib.dmg_split_run_batch(self.h, int(direction), ctypes.c_void_p(stream or 0), n, D, W, S),
+              "dmg_split_run_batch")
+
+    @property
+    def extent64(self):
+        return self.lib.dmg_split_extent64(self.h)
+
     def set_schedule(self, schedule):
         """SCHEDULE_AUTO, SCHEDULE_LINES (one pass per dimension) or SCHEDULE_SPLIT (two per dimension)."""
         check(self.lib.dmg_split_set_schedule(self.h, int(schedule)), "dmg_split_set_schedule")
@@ -506,3 +520,77 @@ def read_file(path: str, decomp: "Decomp", elem_size: int, dst_ptr: int, stream=
     """Read a global C-order file into the distributed array (the reference's readFile)."""
     check(load().dmg_io_read_file(path.encode(), decomp.h, int(elem_size), ctypes.c_void_p(dst_ptr),
                                   ctypes.c_void_p(stream)), "dmg_io_read_file")
+
+
+# ---------------------------------------------------------------- request server
+
+class _JobDesc(ctypes.Structure):
+    _fields_ = [("side", ctypes.c_int), ("dtype", ctypes.c_int), ("input", ctypes.c_void_p),
+                ("spectrum", ctypes.c_void_p), ("output", ctypes.c_void_p)]
+
+
+class _JobDone(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_longlong), ("t_submit", ctypes.c_double), ("t_start", ctypes.c_double),
+                ("t_done", ctypes.c_double), ("batch", ctypes.c_int), ("status", ctypes.c_int)]
+
+
+class Server:
+    """dmg_server_*: reshape + split-FFT jobs of mixed sizes with admission by free HBM, plan caching,
+    stream slots and same-shape batching (include/dmg_serve.h)."""
+
+    def __init__(self, grid=4, arena_bytes=8 << 30, slots=4, max_batch=8):
+        self.lib = load()
+        self.h = self.lib.dmg_server_create(int(grid), int(arena_bytes), int(slots), int(max_batch))
+        if not self.h:
+            raise DecompError("dmg_server_create: %s" % last_error())
+        self.grid = grid
+
+    def sizes(self, side, dtype):
+        """Element counts of a job's host arrays: (input, spectrum, output)."""
+        a, b, c = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
+        check(self.lib.dmg_server_job_sizes(self.h, int(side), int(dtype), ctypes.byref(a), ctypes.byref(b),
+                                            ctypes.byref(c)), "dmg_server_job_sizes")
+        return a.value, b.value, c.value
+
+    def submit(self, side, dtype, input_ptr, spectrum_ptr=0, output_ptr=0):
+        j = _JobDesc(int(side), int(dtype), ctypes.c_void_p(input_ptr), ctypes.c_void_p(spectrum_ptr or None),
+                     ctypes.c_void_p(output_ptr or None))
+        jid = self.lib.dmg_server_submit(self.h, ctypes.byref(j))
+        if jid < 0:
+            raise DecompError("dmg_server_submit: %s" % last_error())
+        return jid
+
+    def poll(self, max_jobs=4096):
+        buf = (_JobDone * max_jobs)()
+        n = self.lib.dmg_server_poll(self.h, buf, max_jobs)
+        if n < 0:
+            raise DecompError("dmg_server_poll: %s" % last_error())
+        return [{"id": d.id, "t_submit": d.t_submit, "t_start": d.t_start, "t_done": d.t_done, "batch": d.batch,
+                 "status": d.status} for d in buf[:n]]
+
+    def drain(self):
+        check(self.lib.dmg_server_drain(self.h), "dmg_server_drain")
+
+    def status(self):
+        q, r, u = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
+        check(self.lib.dmg_server_status(self.h, ctypes.byref(q), ctypes.byref(r), ctypes.byref(u)),
+              "dmg_server_status")
+        return {"queued": q.value, "running": r.value, "arena_used": u.value}
+
+    def close(self):
+        if self.h:
+            self.lib.dmg_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def cube_specs(side, grid=4):
+    """The served jobs' decompositions: (block spec, rotate spec)."""
+    blk = "packed:block(%d,%d)|block(%d,%d)|local(%d)" % (side, grid, side, grid, side)
+    rot = "packed:rotate(%d,block(%d,%d))|rotate(1,block(%d,%d))|local(%d)" % (side // 3, side, grid, side, grid, side)
+    return blk, rot

@@ -55,6 +55,17 @@ int dmg_dev_upload(void *dst, const void *src, size_t bytes);
 void *dmg_current_stream(void);
 int dmg_copy_sync(void *dst, const void *src, size_t bytes, int to_host, void *stream);
 int dmg_stream_sync(void *stream);
+int dmg_rt_stream_create(void **s);
+void dmg_rt_stream_destroy(void *s);
+int dmg_rt_event_create(void **ev);
+void dmg_rt_event_destroy(void *ev);
+int dmg_rt_event_record(void *ev, void *s);
+int dmg_rt_event_done(void *ev);
+int dmg_rt_copy_async(void *dst, const void *src, size_t bytes, int kind, void *s);
+int dmg_rt_copy2d_async(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, size_t height,
+                        int kind, void *s);
+int dmg_rt_get_device(int *dev);
+int dmg_rt_set_device(int dev);
 
 #ifdef __cplusplus
 }

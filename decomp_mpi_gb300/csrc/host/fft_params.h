@@ -84,9 +84,23 @@ struct dmg_fft_pass {
 #define DMG_FFT_TILE_MAX 4096
 #define DMG_FFT_TILE_TARGET(es) ((es) == 8 ? 4096 : 2048)
 
+/* Jobs of one batched launch: the same pass (same plan, so the same tables)
+ * over several arrays.  scale_exp: per job, for double-float passes that
+ * read or write complex128. */
+#define DMG_FFT_MAXBATCH 16
+struct dmg_fft_batch {
+  int32_t count;
+  const void *src[DMG_FFT_MAXBATCH];
+  void *dst[DMG_FFT_MAXBATCH];
+  const int32_t *scale_exp[DMG_FFT_MAXBATCH];
+};
+
 #ifdef __cplusplus
 extern "C" {
 #endif
+/* One launch of a pass over every job of a batch (the tiles of all jobs
+ * share the persistent blocks). */
+int dmg_fft_pass_launch_batch(const struct dmg_fft_pass *p, int dtype, const struct dmg_fft_batch *b, void *stream);
 /* dtype 0: complex128 in FP64 arithmetic, 1: complex64 in FP32, 2: complex128
  * data in double-float (FP32 pair) arithmetic. */
 int dmg_fft_pass_launch(const struct dmg_fft_pass *p, int dtype, const void *src, void *dst, void *stream);

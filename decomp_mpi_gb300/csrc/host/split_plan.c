@@ -985,6 +985,8 @@ int dmg_split_set_arith(SplitPlan plan, int arith) {
 
 int dmg_split_get_arith(SplitPlan plan) { return plan ? plan->impl->arith : -1; }
 
+long long dmg_split_extent64(SplitPlan plan) { return plan ? plan->impl->ext : -1; }
+
 int dmg_split_set_schedule(SplitPlan plan, int schedule) {
   if (!plan) return dmg_error(DMG_ERR_ARG, "dmg_split_set_schedule: NULL plan");
   if (schedule != DMG_SCHEDULE_AUTO && schedule != DMG_SCHEDULE_LINES && schedule != DMG_SCHEDULE_SPLIT)
@@ -1103,6 +1105,61 @@ int dmg_split_run(SplitPlan plan, int direction, void *stream) {
 }
 
 void runSplitPlan(SplitPlan plan, int direction) { dmg_split_run(plan, direction, dmg_current_stream()); }
+
+int dmg_split_run_batch(SplitPlan plan, int direction, void *stream, int count, void *const *dats, void *const *works,
+                        int *const *scales) {
+  if (!plan) return dmg_error(DMG_ERR_ARG, "dmg_split_run_batch: NULL plan");
+  struct dmg_split_impl *im = plan->impl;
+  if (direction != FFTW_FORWARD && direction != FFTW_BACKWARD)
+    return dmg_error(DMG_ERR_ARG, "dmg_split_run_batch: direction %d", direction);
+  if (count < 1 || count > DMG_FFT_MAXBATCH)
+    return dmg_error(DMG_ERR_ARG, "dmg_split_run_batch: %d jobs (1 to %d)", count, DMG_FFT_MAXBATCH);
+  for (int j = 0; j < count; ++j)
+    if (!dats[j] || !works[j] || (im->arith == DMG_ARITH_DF && !scales[j]))
+      return dmg_error(DMG_ERR_ARG, "dmg_split_run_batch: NULL buffer for job %d", j);
+  if (im->nfwd == 0) return dmg_error(DMG_ERR_UNSUPPORTED, "dmg_split_run_batch: the plan has no transform passes");
+  if (!im->dev_valid) {
+    int st = impl_upload(im);
+    if (st != DMG_OK) return st;
+  }
+  pass_rec *list = direction == FFTW_FORWARD ? im->fwd : im->inv;
+  int cnt = direction == FFTW_FORWARD ? im->nfwd : im->ninv;
+  int dt = arith_dtype(im);
+  if (im->arith == DMG_ARITH_DF) {
+    int32_t L[DMG_FFT_MAXDIM], A[DMG_FFT_MAXDIM];
+    for (int d = 0; d < DMG_FFT_MAXDIM; ++d) {
+      L[d] = im->L[d];
+      A[d] = im->A[d];
+    }
+    for (int j = 0; j < count; ++j) {
+      const void *src = list[0].in_buf == BUF_DAT ? dats[j] : works[j];
+      int st = dmg_fft_maxexp_launch(&list[0].p.in, im->ndim, A, L, src, scales[j], stream);
+      if (st != DMG_OK) return st;
+    }
+  }
+  struct dmg_fft_batch b;
+  memset(&b, 0, sizeof(b));
+  b.count = count;
+  for (int k = 0; k < cnt; ++k) {
+    for (int j = 0; j < count; ++j) {
+      b.src[j] = list[k].in_buf == BUF_DAT ? dats[j] : works[j];
+      b.dst[j] = list[k].out_buf == BUF_DAT ? dats[j] : works[j];
+      b.scale_exp[j] = scales ? scales[j] : NULL;
+    }
+    int st = dmg_fft_pass_launch_batch(&list[k].p, dt, &b, stream);
+    if (st != DMG_OK) return st;
+  }
+  return DMG_OK;
+}
+
+int dmg_split_batch_launches(SplitPlan plan, int direction, int count) {
+  if (!plan) return 0;
+  int k = direction == FFTW_FORWARD ? plan->impl->nfwd : plan->impl->ninv;
+  if (plan->impl->arith == DMG_ARITH_DF) k += 2 * count; /* exponent pre-pass: a memset and a kernel per job */
+  return k;
+}
+
+
 
 /* ---------------------------------------------------------------- no-allocation run */
 

@@ -6,9 +6,9 @@
 size_t dmg_fft_pass_smem_f64(const dmg_fft_pass *p);
 size_t dmg_fft_pass_smem_f32(const dmg_fft_pass *p);
 size_t dmg_fft_pass_smem_df(const dmg_fft_pass *p);
-int dmg_fft_pass_launch_f64(const dmg_fft_pass *p, const void *src, void *dst, void *stream);
-int dmg_fft_pass_launch_f32(const dmg_fft_pass *p, const void *src, void *dst, void *stream);
-int dmg_fft_pass_launch_df(const dmg_fft_pass *p, const void *src, void *dst, void *stream);
+int dmg_fft_pass_launch_f64(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream);
+int dmg_fft_pass_launch_f32(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream);
+int dmg_fft_pass_launch_df(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream);
 
 namespace {
 
@@ -42,19 +42,26 @@ extern "C" size_t dmg_fft_pass_smem(const dmg_fft_pass *p, int dtype) {
   return dtype == 0 ? dmg_fft_pass_smem_f64(p) : dtype == 1 ? dmg_fft_pass_smem_f32(p) : dmg_fft_pass_smem_df(p);
 }
 
-extern "C" int dmg_fft_pass_launch(const dmg_fft_pass *p, int dtype, const void *src, void *dst, void *stream) {
+extern "C" int dmg_fft_pass_launch_batch(const dmg_fft_pass *p, int dtype, const dmg_fft_batch *b, void *stream) {
   if ((int64_t)p->M1 * p->M2 * p->n > DMG_FFT_TILE_MAX)
     return dmg_error(DMG_ERR_ARG, "fft tile %d exceeds %d", p->M1 * p->M2 * p->n, DMG_FFT_TILE_MAX);
   if ((p->perm_in || p->perm_out) && (p->perm_a < 1 || p->perm_b < 1 || (int64_t)p->perm_a * p->perm_b != p->n))
     return dmg_error(DMG_ERR_ARG, "fft slot order %d x %d does not match length %d", p->perm_a, p->perm_b, p->n);
-  if (dtype == 2 && (p->in_fp64 || p->out_fp64) && !p->scale_exp)
-    return dmg_error(DMG_ERR_ARG, "double-float pass without a scale exponent");
   switch (dtype) {
-    case 0: return dmg_fft_pass_launch_f64(p, src, dst, stream);
-    case 1: return dmg_fft_pass_launch_f32(p, src, dst, stream);
-    case 2: return dmg_fft_pass_launch_df(p, src, dst, stream);
+    case 0: return dmg_fft_pass_launch_f64(p, b, stream);
+    case 1: return dmg_fft_pass_launch_f32(p, b, stream);
+    case 2: return dmg_fft_pass_launch_df(p, b, stream);
     default: return dmg_error(DMG_ERR_ARG, "fft dtype %d", dtype);
   }
+}
+
+extern "C" int dmg_fft_pass_launch(const dmg_fft_pass *p, int dtype, const void *src, void *dst, void *stream) {
+  dmg_fft_batch b;
+  b.count = 1;
+  b.src[0] = src;
+  b.dst[0] = dst;
+  b.scale_exp[0] = p->scale_exp;
+  return dmg_fft_pass_launch_batch(p, dtype, &b, stream);
 }
 
 extern "C" int dmg_fft_maxexp_launch(const dmg_fft_layout *lay, int ndim, const int32_t *A, const int32_t *L,

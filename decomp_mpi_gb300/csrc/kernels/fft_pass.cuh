@@ -750,23 +750,29 @@ constexpr int EPT = DMG_FFT_EPT;  // values a thread stores per scatter round
 #endif
 constexpr int MINB = DMG_FFT_MINB;  // resident blocks per SM the register budget allows
 
-// A tile's place in the pass.
+// A tile's place in the pass (and which job of the batch it belongs to).
 struct TileState {
   int yb[DMG_FFT_MAXDIM], zb[DMG_FFT_MAXDIM];
   int lim1, lim2, ytw;
+  int job, sexp;
 };
 
 // Values every phase needs.  They live in shared memory and each phase
 // reads them after a barrier, so that none of them holds a register through
 // the FFT stages.
 struct PassConsts {
-  int ld, M1, d0, mult0, sexp, td, v1_ytd, v2_ytd, in64, out64;
+  int ld, M1, d0, mult0, td, v1_ytd, v2_ytd, in64, out64;
   unsigned buf_a, buf_b, contrib_off, perm_off;
   TileState ts[2];  // the tile being transformed and the one being gathered
 };
 
-__device__ __forceinline__ void tile_state(const dmg_fft_pass &p, int64_t tile, TileState &st) {
-  int64_t t = tile;
+template <typename T>
+__device__ __forceinline__ void tile_state(const dmg_fft_pass &p, const dmg_fft_batch &bt, int64_t tile,
+                                           TileState &st) {
+  st.job = (int)(tile / p.ntiles);
+  // scale exponent of the double-float conversions (bias removed, inputs end below 2)
+  st.sexp = (std::is_same<T, df>::value && (p.in_fp64 || p.out_fp64)) ? __ldg(bt.scale_exp[st.job]) - 1022 : 0;
+  int64_t t = tile - (int64_t)st.job * p.ntiles;
   const int i1 = (int)(t % p.nt1);
   t /= p.nt1;
   const int i2 = (int)(t % p.nt2);
@@ -800,7 +806,7 @@ __device__ __forceinline__ void tile_state(const dmg_fft_pass &p, int64_t tile, 
 // complex128 input of a double-float pass is converted once it is there).
 template <typename T, int NF>
 __device__ __forceinline__ void gather_async(const dmg_fft_pass &p, const PassConsts &kc, const TileState &st,
-                                             const unsigned char *sm, const void *src, int tid) {
+                                             const unsigned char *sm, const dmg_fft_batch &bt, int tid) {
   constexpr bool FIXED = NF > 0;
   const int n = FIXED ? NF : p.n;
   const int ld = kc.ld, M1 = kc.M1;
@@ -818,7 +824,7 @@ __device__ __forceinline__ void gather_async(const dmg_fft_pass &p, const PassCo
   const int64_t *tab0 = p.in.tab[d0] + (yb[d0] + p.A[d0] * zb[d0]);
   const int64_t in0 = p.sep_in ? pin[0] : 0;
   C2<T> *stg = reinterpret_cast<C2<T> *>(const_cast<unsigned char *>(sm));
-  const unsigned char *gsrc = static_cast<const unsigned char *>(src);
+  const unsigned char *gsrc = static_cast<const unsigned char *>(bt.src[st.job]);
   TileWalk w(tid, p.load_pos, n, lim1, lim2);
   for (int e = tid; e < total; e += NT, w.next()) {
     const int c0 = w.coord(p.load_pos[0]), c1 = w.coord(p.load_pos[1]), c2 = w.coord(p.load_pos[2]);
@@ -839,12 +845,12 @@ __device__ __forceinline__ void gather_async(const dmg_fft_pass &p, const PassCo
 
 // NF > 0: length NF with a compile-time schedule; NF == 0: any length.
 template <typename T, int SIGN, int NF>
-__global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p, const void *__restrict__ src,
-                                                            void *__restrict__ dst) {
+__global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p, const dmg_fft_batch bt) {
   constexpr bool FIXED = NF > 0;
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ PassConsts kc;
   const int tid = threadIdx.x;
+  const int64_t ntiles_all = p.ntiles * bt.count;
   if (tid == 0) {
     const SmemLayout S = smem_layout<T>(p, FIXED);
     kc.ld = S.ld;
@@ -863,9 +869,7 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
     kc.v2_ytd = p.kdim[2] == td && !p.kisz[2];
     kc.in64 = p.in_fp64 != 0;
     kc.out64 = p.out_fp64 != 0;
-    // scale exponent of the double-float conversions (bias removed, inputs end below 2)
-    kc.sexp = (std::is_same<T, df>::value && (p.in_fp64 || p.out_fp64)) ? __ldg(p.scale_exp) - 1022 : 0;
-    if (blockIdx.x < p.ntiles) tile_state(p, blockIdx.x, kc.ts[0]);
+    if (blockIdx.x < ntiles_all) tile_state<T>(p, bt, blockIdx.x, kc.ts[0]);
   }
   __syncthreads();
   {
@@ -874,7 +878,7 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
       int16_t *perm = reinterpret_cast<int16_t *>(sm + kc.perm_off);
       for (int i = tid; i < n; i += NT) perm[i] = (int16_t)(i / p.perm_a + p.perm_b * (i % p.perm_a));
     }
-    if (p.sep_in && blockIdx.x < p.ntiles) {
+    if (p.sep_in && blockIdx.x < ntiles_all) {
       int xb[DMG_FFT_MAXDIM];
 #pragma unroll
       for (int d = 0; d < DMG_FFT_MAXDIM; ++d) xb[d] = kc.ts[0].yb[d] + p.A[d] * kc.ts[0].zb[d];
@@ -882,10 +886,10 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
     }
   }
   __syncthreads();
-  if (blockIdx.x < p.ntiles) gather_async<T, NF>(p, kc, kc.ts[0], sm, src, tid);
+  if (blockIdx.x < ntiles_all) gather_async<T, NF>(p, kc, kc.ts[0], sm, bt, tid);
 
   int cur = 0;
-  for (int64_t tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x, cur ^= 1) {
+  for (int64_t tile = blockIdx.x; tile < ntiles_all; tile += gridDim.x, cur ^= 1) {
     const int64_t next = tile + gridDim.x;
     // ---- the tile's values are in the staging buffer ----
     copy_async_wait_all();
@@ -896,7 +900,7 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
       const int ld = kc.ld, M1 = kc.M1;
       const TileState &st = kc.ts[cur];
       const int lim1 = st.lim1, lim2 = st.lim2;
-      const int sexp = kc.sexp;
+      const int sexp = st.sexp;
       const C2<T> *twt = reinterpret_cast<const C2<T> *>(p.tw[kc.td]);
       C2<T> *stg = reinterpret_cast<C2<T> *>(sm);
       const int total = n * M1 * p.M2;
@@ -946,8 +950,8 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
         stage_runtime<T, SIGN>(p, 0, 1, stg, bufA, reinterpret_cast<const C2<T> *>(p.roots), nlines, ld, tid);
       }
     }
-    if (next < p.ntiles) {
-      if (tid == 0) tile_state(p, next, kc.ts[cur ^ 1]);
+    if (next < ntiles_all) {
+      if (tid == 0) tile_state<T>(p, bt, next, kc.ts[cur ^ 1]);
       __syncthreads();
       if (p.sep_in) {
         int xb[DMG_FFT_MAXDIM];
@@ -957,7 +961,7 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
                        reinterpret_cast<int64_t *>(sm + kc.contrib_off));
         __syncthreads();
       }
-      gather_async<T, NF>(p, kc, kc.ts[cur ^ 1], sm, src, tid);
+      gather_async<T, NF>(p, kc, kc.ts[cur ^ 1], sm, bt, tid);
     }
 
     // ---- the other stages: between A and B ----
@@ -1004,7 +1008,8 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
       const int64_t *tab0 = p.out.tab[d0] + (yb[d0] + p.A[d0] * zb[d0]);
       const int64_t out0 = p.sep_out ? pout[0] : 0;
       const bool out64 = kc.out64;
-      const int sexp = kc.sexp;
+      const int sexp = st.sexp;
+      void *dst = bt.dst[st.job];
       const C2<T> *twt = reinterpret_cast<const C2<T> *>(p.tw[kc.td]);
       TileWalk w(tid, p.store_pos, n, lim1, lim2);
       for (int e0 = 0; e0 < total; e0 += NT * EPT) {
@@ -1043,7 +1048,7 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
 }
 
 template <typename T, int SIGN, int NF>
-int launch_k(const dmg_fft_pass &p, const void *src, void *dst, cudaStream_t s) {
+int launch_k(const dmg_fft_pass &p, const dmg_fft_batch &bt, cudaStream_t s) {
   const size_t smem = smem_layout<T>(p, NF > 0).total;
   auto k = fft_pass_kernel<T, SIGN, NF>;
   if (smem > 48 * 1024) {
@@ -1056,47 +1061,53 @@ int launch_k(const dmg_fft_pass &p, const void *src, void *dst, cudaStream_t s) 
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, NT, smem);
   if (per_sm < 1) return dmg_error(DMG_ERR_UNSUPPORTED, "fft pass does not fit on an SM (smem %zu)", smem);
   int64_t grid = (int64_t)nsm * per_sm;
-  if (grid > p.ntiles) grid = p.ntiles;
+  if (grid > p.ntiles * bt.count) grid = p.ntiles * bt.count;
   if (grid < 1) return DMG_OK;
-  k<<<(unsigned)grid, NT, smem, s>>>(p, src, dst);
+  k<<<(unsigned)grid, NT, smem, s>>>(p, bt);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return dmg_error(DMG_ERR_CUDA, "fft pass launch: %s", cudaGetErrorString(e));
   return DMG_OK;
 }
 
 template <typename T, int SIGN>
-int launch_sign(const dmg_fft_pass &p, const void *src, void *dst, cudaStream_t s) {
+int launch_sign(const dmg_fft_pass &p, const dmg_fft_batch &bt, cudaStream_t s) {
   switch (p.n) {
-    case 8: return launch_k<T, SIGN, 8>(p, src, dst, s);
-    case 16: return launch_k<T, SIGN, 16>(p, src, dst, s);
-    case 32: return launch_k<T, SIGN, 32>(p, src, dst, s);
-    case 64: return launch_k<T, SIGN, 64>(p, src, dst, s);
-    case 128: return launch_k<T, SIGN, 128>(p, src, dst, s);
-    case 256: return launch_k<T, SIGN, 256>(p, src, dst, s);
-    case 512: return launch_k<T, SIGN, 512>(p, src, dst, s);
-    case 1024: return launch_k<T, SIGN, 1024>(p, src, dst, s);
-    case 2048: return launch_k<T, SIGN, 2048>(p, src, dst, s);
-    case 48: return launch_k<T, SIGN, 48>(p, src, dst, s);
-    case 96: return launch_k<T, SIGN, 96>(p, src, dst, s);
-    case 120: return launch_k<T, SIGN, 120>(p, src, dst, s);
-    case 160: return launch_k<T, SIGN, 160>(p, src, dst, s);
-    case 192: return launch_k<T, SIGN, 192>(p, src, dst, s);
-    case 240: return launch_k<T, SIGN, 240>(p, src, dst, s);
-    case 320: return launch_k<T, SIGN, 320>(p, src, dst, s);
-    case 384: return launch_k<T, SIGN, 384>(p, src, dst, s);
-    case 480: return launch_k<T, SIGN, 480>(p, src, dst, s);
-    default: return launch_k<T, SIGN, 0>(p, src, dst, s);
+    case 8: return launch_k<T, SIGN, 8>(p, bt, s);
+    case 16: return launch_k<T, SIGN, 16>(p, bt, s);
+    case 32: return launch_k<T, SIGN, 32>(p, bt, s);
+    case 64: return launch_k<T, SIGN, 64>(p, bt, s);
+    case 128: return launch_k<T, SIGN, 128>(p, bt, s);
+    case 256: return launch_k<T, SIGN, 256>(p, bt, s);
+    case 512: return launch_k<T, SIGN, 512>(p, bt, s);
+    case 1024: return launch_k<T, SIGN, 1024>(p, bt, s);
+    case 2048: return launch_k<T, SIGN, 2048>(p, bt, s);
+    case 48: return launch_k<T, SIGN, 48>(p, bt, s);
+    case 96: return launch_k<T, SIGN, 96>(p, bt, s);
+    case 120: return launch_k<T, SIGN, 120>(p, bt, s);
+    case 160: return launch_k<T, SIGN, 160>(p, bt, s);
+    case 192: return launch_k<T, SIGN, 192>(p, bt, s);
+    case 240: return launch_k<T, SIGN, 240>(p, bt, s);
+    case 320: return launch_k<T, SIGN, 320>(p, bt, s);
+    case 384: return launch_k<T, SIGN, 384>(p, bt, s);
+    case 480: return launch_k<T, SIGN, 480>(p, bt, s);
+    default: return launch_k<T, SIGN, 0>(p, bt, s);
   }
 }
 
-// Launch one pass in arithmetic T (checked by the caller).
+// Launch one pass over a batch of jobs in arithmetic T (checked by the caller).
 template <typename T>
-int launch_pass(const dmg_fft_pass &p, const void *src, void *dst, void *stream) {
+int launch_pass(const dmg_fft_pass &p, const dmg_fft_batch &bt, void *stream) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  // the gather copies whole values asynchronously: both arrays need their natural alignment
-  if ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) % sizeof(C2<T>) != 0)
-    return dmg_error(DMG_ERR_ARG, "fft pass: buffers must be aligned to %zu bytes", sizeof(C2<T>));
-  return p.sign < 0 ? launch_sign<T, -1>(p, src, dst, s) : launch_sign<T, 1>(p, src, dst, s);
+  if (bt.count < 1 || bt.count > DMG_FFT_MAXBATCH)
+    return dmg_error(DMG_ERR_ARG, "fft pass: batch of %d jobs (1 to %d)", bt.count, DMG_FFT_MAXBATCH);
+  for (int j = 0; j < bt.count; ++j) {
+    // the gather copies whole values asynchronously: both arrays need their natural alignment
+    if ((reinterpret_cast<uintptr_t>(bt.src[j]) | reinterpret_cast<uintptr_t>(bt.dst[j])) % sizeof(C2<T>) != 0)
+      return dmg_error(DMG_ERR_ARG, "fft pass: buffers must be aligned to %zu bytes", sizeof(C2<T>));
+    if (std::is_same<T, df>::value && (p.in_fp64 || p.out_fp64) && !bt.scale_exp[j])
+      return dmg_error(DMG_ERR_ARG, "double-float pass without a scale exponent");
+  }
+  return p.sign < 0 ? launch_sign<T, -1>(p, bt, s) : launch_sign<T, 1>(p, bt, s);
 }
 
 template <typename T>

@@ -3,6 +3,6 @@
 
 size_t dmg_fft_pass_smem_f32(const dmg_fft_pass *p) { return pass_smem<float>(*p); }
 
-int dmg_fft_pass_launch_f32(const dmg_fft_pass *p, const void *src, void *dst, void *stream) {
-  return launch_pass<float>(*p, src, dst, stream);
+int dmg_fft_pass_launch_f32(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream) {
+  return launch_pass<float>(*p, *b, stream);
 }

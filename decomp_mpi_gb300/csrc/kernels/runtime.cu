@@ -49,6 +49,66 @@ extern "C" int dmg_stream_sync(void *stream) {
   return DMG_OK;
 }
 
+// Streams, events and asynchronous copies for the request server.
+extern "C" int dmg_rt_stream_create(void **s) {
+  cudaStream_t st = nullptr;
+  cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  *s = st;
+  if (e != cudaSuccess) return dmg_error(DMG_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+  return DMG_OK;
+}
+extern "C" void dmg_rt_stream_destroy(void *s) {
+  if (s) cudaStreamDestroy(static_cast<cudaStream_t>(s));
+}
+extern "C" int dmg_rt_event_create(void **ev) {
+  cudaEvent_t e = nullptr;
+  cudaError_t r = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  *ev = e;
+  if (r != cudaSuccess) return dmg_error(DMG_ERR_CUDA, "cudaEventCreate: %s", cudaGetErrorString(r));
+  return DMG_OK;
+}
+extern "C" void dmg_rt_event_destroy(void *ev) {
+  if (ev) cudaEventDestroy(static_cast<cudaEvent_t>(ev));
+}
+extern "C" int dmg_rt_event_record(void *ev, void *s) {
+  cudaError_t r = cudaEventRecord(static_cast<cudaEvent_t>(ev), static_cast<cudaStream_t>(s));
+  if (r != cudaSuccess) return dmg_error(DMG_ERR_CUDA, "cudaEventRecord: %s", cudaGetErrorString(r));
+  return DMG_OK;
+}
+// 1 when the work before the event has completed, 0 while it runs, an error code otherwise
+extern "C" int dmg_rt_event_done(void *ev) {
+  cudaError_t r = cudaEventQuery(static_cast<cudaEvent_t>(ev));
+  if (r == cudaSuccess) return 1;
+  if (r == cudaErrorNotReady) return 0;
+  return -dmg_error(DMG_ERR_CUDA, "cudaEventQuery: %s", cudaGetErrorString(r));
+}
+// kind: 0 host->device, 1 device->host, 2 device->device
+extern "C" int dmg_rt_copy_async(void *dst, const void *src, size_t bytes, int kind, void *s) {
+  const cudaMemcpyKind k = kind == 0 ? cudaMemcpyHostToDevice : kind == 1 ? cudaMemcpyDeviceToHost
+                                                                          : cudaMemcpyDeviceToDevice;
+  cudaError_t r = cudaMemcpyAsync(dst, src, bytes, k, static_cast<cudaStream_t>(s));
+  if (r != cudaSuccess) return dmg_error(DMG_ERR_CUDA, "cudaMemcpyAsync(%zu): %s", bytes, cudaGetErrorString(r));
+  return DMG_OK;
+}
+extern "C" int dmg_rt_copy2d_async(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width,
+                                   size_t height, int kind, void *s) {
+  const cudaMemcpyKind k = kind == 0 ? cudaMemcpyHostToDevice : kind == 1 ? cudaMemcpyDeviceToHost
+                                                                          : cudaMemcpyDeviceToDevice;
+  cudaError_t r = cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, height, k, static_cast<cudaStream_t>(s));
+  if (r != cudaSuccess) return dmg_error(DMG_ERR_CUDA, "cudaMemcpy2DAsync: %s", cudaGetErrorString(r));
+  return DMG_OK;
+}
+extern "C" int dmg_rt_get_device(int *dev) {
+  cudaError_t r = cudaGetDevice(dev);
+  if (r != cudaSuccess) return dmg_error(DMG_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(r));
+  return DMG_OK;
+}
+extern "C" int dmg_rt_set_device(int dev) {
+  cudaError_t r = cudaSetDevice(dev);
+  if (r != cudaSuccess) return dmg_error(DMG_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(r));
+  return DMG_OK;
+}
+
 // CUDA-event pairs used by plan timing and the autotuner.
 struct dmg_events {
   int count;

@@ -153,6 +153,18 @@ int dmg_split_get_arith(SplitPlan plan);
 #define DMG_SCHEDULE_AUTO 0
 #define DMG_SCHEDULE_LINES 1
 #define DMG_SCHEDULE_SPLIT 2
+/** One run of a plan over `count` (at most 16) arrays at once, each with its
+ * own dat and workspace (the plan's own buffers are not used), the passes of
+ * all jobs sharing persistent launches.  scales[j]: a device int per job
+ * for double-float plans (the input's exponent; NULL otherwise).  No
+ * counterpart in the reference (which runs one plan per call). */
+int dmg_split_run_batch(SplitPlan plan, int direction, void *stream, int count, void *const *dats, void *const *works,
+                        int *const *scales);
+/** The plan's extent (largest A / B extent over the ranks) as a 64-bit count;
+ * the workspace needs 2 * extent per rank. */
+long long dmg_split_extent64(SplitPlan plan);
+/** Kernel launches of one dmg_split_run_batch call. */
+int dmg_split_batch_launches(SplitPlan plan, int direction, int count);
 /** Select the pass schedule (no counterpart in the reference). */
 int dmg_split_set_schedule(SplitPlan plan, int schedule);
 /** The schedule in use: DMG_SCHEDULE_LINES or DMG_SCHEDULE_SPLIT. */

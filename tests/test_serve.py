@@ -1,0 +1,156 @@
+"""Batched split-FFT runs and the request server: batched results equal single runs, every job's result is
+the same alone and in a mix of sizes and types, and the results match the FP64 oracle."""
+import numpy as np
+import pytest
+
+from decomp_mpi_gb300 import api
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+GRID = 4
+P = GRID * GRID
+TOL = {api.C128: 1e-12, api.C64: 2e-6}
+
+
+def _rel(a, b):
+    m = float(np.max(np.abs(b)))
+    return float(np.linalg.norm((a - b) / m) / np.linalg.norm(b / m)) if m else float(np.max(np.abs(a)))
+
+
+def _cube(side, dtype, seed):
+    rng = np.random.default_rng(seed)
+    g = rng.uniform(-1, 1, (side,) * 3) + 1j * rng.uniform(-1, 1, (side,) * 3)
+    return g if dtype == api.C128 else g.astype(np.complex64)
+
+
+@pytest.mark.parametrize("dtype", [api.C128, api.C64], ids=["c128", "c64"])
+def test_batched_run_equals_single_runs(dtype, cuda):
+    """dmg_split_run_batch over three arrays gives, bit for bit, what three dmg_split_run calls give."""
+    import torch
+    side = 24
+    _, rot = api.cube_specs(side, GRID)
+    comm = api.Comm(P)
+    D = api.decomp_from_spec(comm, rot)
+    tdt = torch.complex128 if dtype == api.C128 else torch.complex64
+    probe = api.SplitPlan(D, 1 << 20, 1 << 40, 1 << 21, dtype=dtype)
+    length = 2 * probe.extent64
+    probe.free()
+    dats = [torch.from_numpy(O.scatter_global(P, rot, _cube(side, dtype, s), D.extent())).to(cuda) for s in range(3)]
+    works = [torch.zeros(P * length, dtype=tdt, device=cuda) for _ in range(3)]
+    scales = torch.zeros(3 * 64, dtype=torch.int32, device=cuda)
+    sp = api.SplitPlan(D, dats[0].data_ptr(), length, works[0].data_ptr(), dtype=dtype)
+    st = torch.cuda.current_stream().cuda_stream
+    single_w, single_d = [], []
+    for i in range(3):
+        d = dats[i].clone()
+        w = torch.zeros_like(works[i])
+        sp.set_buffers(d.data_ptr(), w.data_ptr())
+        sp.run(api.FFTW_FORWARD, st)
+        single_w.append(w.clone())
+        sp.run(api.FFTW_BACKWARD, st)
+        single_d.append(d)
+    sptr = [scales.data_ptr() + 256 * i for i in range(3)]
+    sp.run_batch(api.FFTW_FORWARD, [d.data_ptr() for d in dats], [w.data_ptr() for w in works], sptr, st)
+    torch.cuda.synchronize()
+    for i in range(3):
+        assert torch.equal(works[i], single_w[i])
+    sp.run_batch(api.FFTW_BACKWARD, [d.data_ptr() for d in dats], [w.data_ptr() for w in works], sptr, st)
+    torch.cuda.synchronize()
+    for i in range(3):
+        assert torch.equal(dats[i], single_d[i])
+
+
+def _job_list():
+    rng = np.random.default_rng(3)
+    sides = [16, 24, 32, 48]
+    return [(int(rng.choice(sides)), api.C128 if rng.random() < 0.5 else api.C64, 100 + i) for i in range(20)]
+
+
+def _run(server, jobs, cuda, one_at_a_time):
+    import torch
+    bufs = []
+    for side, dtype, seed in jobs:
+        blk, _ = api.cube_specs(side, GRID)
+        n_in, n_spec, n_out = server.sizes(side, dtype)
+        npdt = np.complex128 if dtype == api.C128 else np.complex64
+        comm = api.Comm(P)
+        pitch = api.decomp_from_spec(comm, blk).extent()
+        host_in = torch.from_numpy(O.scatter_global(P, blk, _cube(side, dtype, seed), pitch).astype(npdt)).pin_memory()
+        assert host_in.numel() == n_in
+        spec = torch.zeros(n_spec, dtype=host_in.dtype).pin_memory()
+        out = torch.zeros(n_out, dtype=host_in.dtype).pin_memory()
+        bufs.append((host_in, spec, out))
+    done = []
+    for (side, dtype, _), (hi, hs, ho) in zip(jobs, bufs):
+        server.submit(side, dtype, hi.data_ptr(), hs.data_ptr(), ho.data_ptr())
+        if one_at_a_time:
+            server.drain()
+    server.drain()
+    done += server.poll()
+    assert len(done) == len(jobs) and all(d["status"] == 0 for d in done)
+    return bufs, done
+
+
+def test_results_alone_equal_results_in_the_mix(cuda):
+    """Each job's spectrum and inverse are the same run alone (one slot, no batching, one job at a time)
+    and run in a mix (several slots, batching, all submitted at once)."""
+    jobs = _job_list()
+    alone = api.Server(GRID, 1 << 30, slots=1, max_batch=1)
+    a_bufs, _ = _run(alone, jobs, cuda, one_at_a_time=True)
+    alone.close()
+    mix = api.Server(GRID, 1 << 30, slots=3, max_batch=8)
+    m_bufs, m_done = _run(mix, jobs, cuda, one_at_a_time=False)
+    mix.close()
+    assert max(d["batch"] for d in m_done) > 1  # some launches were shared
+    srv = api.Server(GRID, 1 << 26, slots=1, max_batch=1)
+    for (side, dtype, _), a, m in zip(jobs, a_bufs, m_bufs):
+        # the same kernels on the same data: identical bits in every slot a rank holds
+        spec_held, out_held = _held(srv, side, dtype)
+        assert np.array_equal(a[1].numpy()[spec_held], m[1].numpy()[spec_held])
+        assert np.array_equal(a[2].numpy()[out_held], m[2].numpy()[out_held])
+    srv.close()
+
+
+def _held(server, side, dtype):
+    """Masks of the spectrum and output slots some rank holds (the rest is padding)."""
+    _, rot = api.cube_specs(side, GRID)
+    n_in, n_spec, n_out = server.sizes(side, dtype)
+    ext = n_spec // P
+    _, mask = O.split_expected_output(P, rot, np.zeros((side,) * 3), 2 * ext)
+    spec = mask.reshape(P, 2 * ext)[:, :ext].ravel()
+    out = np.zeros(n_out, dtype=bool)
+    out[O.global_offsets(P, rot, n_out // P, (side,) * 3).ravel()] = True
+    return spec, out
+
+
+def test_server_results_match_oracle(cuda):
+    """Spectrum against the FP64 oracle in the plan's B slots, inverse back to N times the input."""
+    jobs = [(24, api.C128, 7), (24, api.C64, 8), (48, api.C128, 9), (16, api.C64, 10)]
+    srv = api.Server(GRID, 1 << 30, slots=2, max_batch=4)
+    bufs, _ = _run(srv, jobs, cuda, one_at_a_time=False)
+    for (side, dtype, seed), (hi, hs, ho) in zip(jobs, bufs):
+        blk, rot = api.cube_specs(side, GRID)
+        g = _cube(side, dtype, seed).astype(np.complex128)
+        n_in, n_spec, n_out = srv.sizes(side, dtype)
+        ext = n_spec // P
+        exp, mask = O.split_expected_output(P, rot, g, 2 * ext)
+        exp = exp.reshape(P, 2 * ext)[:, :ext].ravel()
+        mask = mask.reshape(P, 2 * ext)[:, :ext].ravel()
+        got = hs.numpy().astype(np.complex128)
+        assert _rel(got[mask], exp[mask]) < TOL[dtype]
+        comm = api.Comm(P)
+        pitch_rot = api.decomp_from_spec(comm, rot).extent()
+        back = O.gather_global(P, rot, ho.numpy().astype(np.complex128), pitch_rot, (side,) * 3) / side ** 3
+        assert _rel(back, g) < TOL[dtype]
+    srv.close()
+
+
+def test_server_refuses_a_job_larger_than_the_arena(cuda):
+    srv = api.Server(GRID, 1 << 20, slots=1, max_batch=1)
+    import torch
+    n_in, _, _ = srv.sizes(64, api.C128)
+    x = torch.zeros(n_in, dtype=torch.complex128).pin_memory()
+    with pytest.raises(RuntimeError):
+        srv.submit(64, api.C128, x.data_ptr())
+    srv.close()
