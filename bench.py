@@ -665,6 +665,7 @@ def run_precision(args):
         return statistics.median(ms)
 
     ms32 = timed(sp64)
+    sched64 = "lines" if sp64.schedule == api.SCHEDULE_LINES else "split"
     B = sp64.decomp_B()
     spec32 = w64.view(Pp, length)[:, :ext].contiguous()
     out32 = torch.empty(N, dtype=torch.complex64, device=dev)
@@ -698,7 +699,8 @@ def run_precision(args):
     line = {
         "metric": "precision form: split 3D FFT of 1024^3 complex64, error against an FP64-accuracy transform",
         "config": {"n": n, "grid": "8x8 virtual", "input": "complex N(0,1), seed 2, + 16 unit plane waves (seed 2)",
-                   "schedule": "lines" if sp128.schedule == api.SCHEDULE_LINES else "split"},
+                   "schedule_c64": sched64,
+                   "schedule_c128": "lines" if sp128.schedule == api.SCHEDULE_LINES else "split"},
         "fp32": {"ms": round(ms32, 3), "gflops": round(flops / (ms32 * 1e-3) / 1e9, 1),
                  "hbm_gbs": round(6 * N * 8 / (ms32 * 1e-3) / 1e9, 1),
                  "hbm_note": "three passes, each reading and writing the array once (6 N * 8 bytes)"},

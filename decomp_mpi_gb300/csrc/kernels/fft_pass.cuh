@@ -802,6 +802,73 @@ __device__ __forceinline__ void tile_state(const dmg_fft_pass &p, const dmg_fft_
   st.lim2 = p.v2 >= 0 ? min(p.M2, p.nv2 - i2 * p.M2) : 1;
 }
 
+// Visits the values of a tile that thread `tid` owns on a separable side,
+// calling f(address, staging position, c0, c1, c2).  Warps run along the
+// walk's fastest axis (order[0], the one contiguous in the layout).  When that
+// axis is at most NT long, each thread keeps one fast coordinate (and its
+// address part) for the whole tile and steps over rows; when it is longer,
+// each thread keeps up to 8 fast coordinates and loops over rows.  Address
+// parts: the transform axis's from its table (tab0, step mult0), the vector
+// axes' from the per-tile table `part`.  Returns false (visiting nothing)
+// when the fast axis is longer than 8 * NT.
+template <typename T, int NF, typename F>
+__device__ __forceinline__ bool sep_walk(const int32_t *order, int n, int lim1, int lim2, int M1, int ld,
+                                         const int64_t *tab0, int mult0, int64_t base, const int64_t *part,
+                                         const int16_t *perm, bool use_perm, int tid, F &&f) {
+  const int kf = order[0], km = order[1], ks = order[2];
+  auto E = [&](int k) { return k == 0 ? n : (k == 1 ? lim1 : lim2); };
+  auto AP = [&](int k, int i) -> int64_t { return k == 0 ? __ldg(tab0 + i * mult0) : part[k == 1 ? 1 + i : 1 + M1 + i]; };
+  auto SP = [&](int k, int i) -> int {
+    return k == 0 ? swz<T, NF>(use_perm ? (int)perm[i] : i) : (k == 1 ? i * ld : i * M1 * ld);
+  };
+  auto C = [&](int k, int i_f, int i_m, int i_s) { return kf == k ? i_f : (km == k ? i_m : i_s); };
+  const int ef = E(kf), em = E(km), es = E(ks);
+  const int rows = em * es;
+  if (ef <= NT) {
+    const int rstep = NT / ef;
+    if (tid >= rstep * ef) return true;
+    const int i_f = tid % ef;
+    const int64_t af = base + AP(kf, i_f);
+    const int sf = SP(kf, i_f);
+    if (es == 1) {
+      const int64_t a1 = af + AP(ks, 0);
+      const int s1 = sf + SP(ks, 0);
+#pragma unroll 4
+      for (int r = tid / ef; r < rows; r += rstep)
+        f(a1 + AP(km, r), s1 + SP(km, r), C(0, i_f, r, 0), C(1, i_f, r, 0), C(2, i_f, r, 0));
+    } else {
+      for (int r = tid / ef; r < rows; r += rstep) {
+        const int i_m = r % em, i_s = r / em;
+        f(af + AP(km, i_m) + AP(ks, i_s), sf + SP(km, i_m) + SP(ks, i_s), C(0, i_f, i_m, i_s), C(1, i_f, i_m, i_s),
+          C(2, i_f, i_m, i_s));
+      }
+    }
+    return true;
+  }
+  if (ef > 8 * NT) return false;
+  int64_t af[8];
+  int sf[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int i_f = tid + j * NT;
+    if (i_f < ef) {
+      af[j] = base + AP(kf, i_f);
+      sf[j] = SP(kf, i_f);
+    }
+  }
+  for (int r = 0; r < rows; ++r) {
+    const int i_m = r % em, i_s = r / em;
+    const int64_t ar = AP(km, i_m) + AP(ks, i_s);
+    const int sr = SP(km, i_m) + SP(ks, i_s);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int i_f = tid + j * NT;
+      if (i_f < ef) f(af[j] + ar, sf[j] + sr, C(0, i_f, i_m, i_s), C(1, i_f, i_m, i_s), C(2, i_f, i_m, i_s));
+    }
+  }
+  return true;
+}
+
 // Start the copies of a tile into the staging buffer (raw values: a
 // complex128 input of a double-float pass is converted once it is there).
 template <typename T, int NF>
@@ -825,6 +892,14 @@ __device__ __forceinline__ void gather_async(const dmg_fft_pass &p, const PassCo
   const int64_t in0 = p.sep_in ? pin[0] : 0;
   C2<T> *stg = reinterpret_cast<C2<T> *>(const_cast<unsigned char *>(sm));
   const unsigned char *gsrc = static_cast<const unsigned char *>(bt.src[st.job]);
+  if (p.sep_in &&
+      sep_walk<T, NF>(p.load_order, n, lim1, lim2, M1, ld, tab0, mult0, in0, pin, perm, p.perm_in != 0, tid,
+                      [&](int64_t ad, int sp, int, int, int) {
+                        copy_async<sizeof(C2<T>)>(stg + sp, gsrc + ad * (int64_t)sizeof(C2<T>));
+                      })) {
+    copy_async_commit();
+    return;
+  }
   TileWalk w(tid, p.load_pos, n, lim1, lim2);
   for (int e = tid; e < total; e += NT, w.next()) {
     const int c0 = w.coord(p.load_pos[0]), c1 = w.coord(p.load_pos[1]), c2 = w.coord(p.load_pos[2]);
@@ -1011,8 +1086,20 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
       const int sexp = st.sexp;
       void *dst = bt.dst[st.job];
       const C2<T> *twt = reinterpret_cast<const C2<T> *>(p.tw[kc.td]);
+      const bool tw1 = p.twiddle == 1;
+      const int ytw = st.ytw, v1y = kc.v1_ytd, v2y = kc.v2_ytd;
+      bool done = p.sep_out &&
+                  sep_walk<T, NF>(p.store_order, n, lim1, lim2, M1, ld, tab0, mult0, out0, pout, perm,
+                                  p.perm_out != 0, tid, [&](int64_t ad, int sp, int c0, int c1, int c2) {
+                                    C2<T> x = res[sp];
+                                    if (tw1) {
+                                      const int ex = (ytw + (v1y ? c1 : 0) + (v2y ? c2 : 0)) * c0;
+                                      if (ex) x = mul<T>(x, twt[ex]);
+                                    }
+                                    store_elem<T>(dst, ad, x, out64, sexp);
+                                  });
       TileWalk w(tid, p.store_pos, n, lim1, lim2);
-      for (int e0 = 0; e0 < total; e0 += NT * EPT) {
+      for (int e0 = 0; !done && e0 < total; e0 += NT * EPT) {
         int64_t ad[EPT];
         C2<T> v[EPT];
         bool ok[EPT];
