@@ -451,10 +451,11 @@ static int impl_upload(struct dmg_split_impl *im) {
         /* double-float: each component as hi + lo floats */
         long double c = cosl(a), sn = sinl(a);
         float ch = (float)c, sh = (float)sn;
+        /* (re.hi, im.hi, re.lo, im.lo): the kernels' paired layout */
         float *f = (float *)(host + pos) + 4 * i;
         f[0] = ch;
-        f[1] = (float)(c - (long double)ch);
-        f[2] = sh;
+        f[1] = sh;
+        f[2] = (float)(c - (long double)ch);
         f[3] = (float)(sn - (long double)sh);
       } else if (cs == 16) {
         ((double *)(host + pos))[2 * i] = (double)cosl(a);
@@ -475,9 +476,9 @@ static int impl_upload(struct dmg_split_impl *im) {
       if (im->arith == DMG_ARITH_DF) {
         float *f = (float *)(host + pos) + 4 * m;
         f[0] = (float)re;
-        f[1] = (float)(re - (double)f[0]);
-        f[2] = (float)iv;
-        f[3] = (float)(iv - (double)f[2]);
+        f[1] = (float)iv;
+        f[2] = (float)(re - (double)f[0]);
+        f[3] = (float)(iv - (double)f[1]);
       } else if (cs == 16) {
         ((double *)(host + pos))[2 * m] = re;
         ((double *)(host + pos))[2 * m + 1] = iv;

@@ -37,7 +37,9 @@
 // exponent, so every value fits FP32's exponent range) and the last pass
 // converts back and scales by 2^E, both with integer operations.
 // Error-free transformations used: Knuth's two-sum for addition, the FMA
-// product error for multiplication.
+// product error for multiplication.  FP32 and double-float complex values
+// keep (re, im) in one float pair, so that their arithmetic runs as
+// Blackwell's paired FP32 instructions (one instruction per pair).
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
@@ -49,6 +51,20 @@ namespace {
 
 constexpr int NT = DMG_FFT_NT;
 constexpr int TILE_MAX = DMG_FFT_TILE_MAX;
+
+// ---------------------------------------------------------------- paired FP32 operations
+
+// Blackwell's two-wide FP32 instructions (FADD2, FMUL2, FFMA2): each runs
+// one operation on both floats of a pair, rounding each as its scalar form.
+// Complex values keep (re, im) in one pair so that every complex operation
+// is a sequence of paired instructions.
+__device__ __forceinline__ float2 p2(float x, float y) { return make_float2(x, y); }
+__device__ __forceinline__ float2 splat(float x) { return make_float2(x, x); }
+__device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+// a - b as an FMA with -1 (exact product, one rounding: the same as a subtraction)
+__device__ __forceinline__ float2 psub(float2 a, float2 b) { return __ffma2_rn(b, splat(-1.0f), a); }
+__device__ __forceinline__ float2 pmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 
 // ---------------------------------------------------------------- double-float reals
 
@@ -79,8 +95,12 @@ __device__ __forceinline__ df operator*(df a, df b) {
 
 // ---------------------------------------------------------------- complex types
 
+// A double-float complex number: the leading parts (re, im) in one pair and
+// the trailing parts in another, so that the two-sum and product-error steps
+// of the real and imaginary parts run as paired instructions.  Stored in
+// shared memory and HBM in the same order (re.hi, im.hi, re.lo, im.lo).
 struct dfc {
-  df x, y;
+  float2 h, l;
 };
 template <typename T>
 struct CT;
@@ -99,7 +119,7 @@ struct CT<df> {
 template <typename T>
 using C2 = typename CT<T>::type;
 
-// a constant in each arithmetic: v for FP64 and FP32, (hi, lo) for double-float
+// a real constant in each arithmetic: v for FP64 and FP32, (hi, lo) for double-float
 template <typename T>
 __device__ __forceinline__ T cst(double v, float hi, float lo);
 template <>
@@ -115,89 +135,126 @@ __device__ __forceinline__ df cst<df>(double, float hi, float lo) {
   return df{hi, lo};
 }
 
-template <typename T>
-__device__ __forceinline__ C2<T> mk(T x, T y) {
-  C2<T> r;
-  r.x = x;
-  r.y = y;
-  return r;
+// --- FP64: scalar ---
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
-template <typename T>
-__device__ __forceinline__ C2<T> add(C2<T> a, C2<T> b) { return mk<T>(a.x + b.x, a.y + b.y); }
-template <typename T>
-__device__ __forceinline__ C2<T> sub(C2<T> a, C2<T> b) { return mk<T>(a.x - b.x, a.y - b.y); }
-template <typename T>
-__device__ __forceinline__ C2<T> mul(C2<T> a, C2<T> b) {
-  return mk<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+__device__ __forceinline__ double2 cscl(double2 a, double c) { return make_double2(a.x * c, a.y * c); }
+__device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+template <int SIGN>
+__device__ __forceinline__ double2 crot(double2 a) {  // multiply by sign * i
+  return SIGN < 0 ? make_double2(a.y, -a.x) : make_double2(-a.y, a.x);
 }
 
-#ifndef DMG_DF_FUSED
-#define DMG_DF_FUSED 1
-#endif
-#if DMG_DF_FUSED
-// a*b + c*d in double-float with one renormalisation: the two leading
-// products and their exact errors (FMA), the exact sum of the leading
-// products (two-sum), and the cross terms; the a.l*b.l terms (2^-48 of the
-// result) are dropped as in the plain product.  19 FP32 operations.
-__device__ __forceinline__ df df_dot2(df a, df b, df c, df d) {
-  const float p1 = a.h * b.h;
-  const float p2 = c.h * d.h;
-  const float e1 = fmaf(a.h, b.h, -p1);
-  const float e2 = fmaf(c.h, d.h, -p2);
-  const float s = p1 + p2;
-  const float v = s - p1;
-  float t = (p1 - (s - v)) + (p2 - v);
-  t += e1 + e2;
-  t = fmaf(a.h, b.l, t);
-  t = fmaf(a.l, b.h, t);
-  t = fmaf(c.h, d.l, t);
-  t = fmaf(c.l, d.h, t);
-  return df_norm(s, t);
+// --- FP32: paired ---
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return padd(a, b); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return psub(a, b); }
+// a * b = a.x * (b.x, b.y) + a.y * (-b.y, b.x)
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return pfma(splat(a.y), p2(-b.y, b.x), pmul(splat(a.x), b));
 }
-template <>
-__device__ __forceinline__ dfc mul<df>(dfc a, dfc b) {
-  return dfc{df_dot2(a.x, b.x, -a.y, b.y), df_dot2(a.x, b.y, a.y, b.x)};
+__device__ __forceinline__ float2 cscl(float2 a, float c) { return pmul(a, splat(c)); }
+__device__ __forceinline__ float2 cconj(float2 a) { return p2(a.x, -a.y); }
+template <int SIGN>
+__device__ __forceinline__ float2 crot(float2 a) {
+  return SIGN < 0 ? p2(a.y, -a.x) : p2(-a.y, a.x);
 }
-#endif
 
-// Sum and difference whose double-float result is left unnormalised (the
-// two-sum of the leading parts plus the trailing parts, 8 operations instead
-// of 11); used where the result only feeds further additions.  Exact FP64 and
-// FP32 arithmetic is unaffected.
-#ifndef DMG_DF_LAZY
-#define DMG_DF_LAZY 1
-#endif
-__device__ __forceinline__ df df_add_lazy(df a, df b) {
-  const float s = a.h + b.h;
-  const float v = s - a.h;
-  float e = (a.h - (s - v)) + (b.h - v);
-  e += a.l + b.l;
-  return df{s, e};
+// --- double-float: paired two-sum / FMA product error ---
+__device__ __forceinline__ dfc dnorm(float2 s, float2 e) {  // fast two-sum of both lanes, |s| >= |e|
+  const float2 h = padd(s, e);
+  return dfc{h, psub(e, psub(h, s))};
 }
+// sum with the result left unnormalised (two-sum of the leading parts plus
+// the trailing parts); for results that only feed further additions
+__device__ __forceinline__ dfc cadd_lazy(dfc a, dfc b) {
+  const float2 s = padd(a.h, b.h);
+  const float2 v = psub(s, a.h);
+  float2 e = padd(psub(a.h, psub(s, v)), psub(b.h, v));
+  e = padd(e, padd(a.l, b.l));
+  return dfc{s, e};
+}
+__device__ __forceinline__ dfc cadd(dfc a, dfc b) {
+  const dfc r = cadd_lazy(a, b);
+  return dnorm(r.h, r.l);
+}
+// difference: the two-sum of a and -b
+__device__ __forceinline__ dfc csub_lazy(dfc a, dfc b) {
+  const float2 s = psub(a.h, b.h);
+  const float2 v = psub(s, a.h);
+  const float2 e = psub(psub(a.h, psub(s, v)), padd(b.h, v));
+  return dfc{s, padd(e, psub(a.l, b.l))};
+}
+__device__ __forceinline__ dfc csub(dfc a, dfc b) {
+  const dfc r = csub_lazy(a, b);
+  return dnorm(r.h, r.l);
+}
+// a * b = a.re * b + a.im * (i b): the leading products and their exact
+// errors (FMA), the exact sum of the leading products (two-sum), the cross
+// terms; the lo*lo terms (2^-48 of the result) are dropped
+__device__ __forceinline__ dfc cmul(dfc a, dfc b) {
+  const float2 bh_i = p2(-b.h.y, b.h.x), bl_i = p2(-b.l.y, b.l.x);
+  const float2 xh = splat(a.h.x), yh = splat(a.h.y), xl = splat(a.l.x), yl = splat(a.l.y);
+  const float2 q1 = pmul(xh, b.h);
+  const float2 q2 = pmul(yh, bh_i);
+  const float2 e1 = pfma(xh, b.h, p2(-q1.x, -q1.y));
+  const float2 e2 = pfma(yh, bh_i, p2(-q2.x, -q2.y));
+  const float2 s = padd(q1, q2);
+  const float2 v = psub(s, q1);
+  float2 t = padd(psub(q1, psub(s, v)), psub(q2, v));
+  t = padd(t, padd(e1, e2));
+  t = pfma(xh, b.l, t);
+  t = pfma(xl, b.h, t);
+  t = pfma(yh, bl_i, t);
+  t = pfma(yl, bh_i, t);
+  return dnorm(s, t);
+}
+// a * c for a real double-float constant c
+__device__ __forceinline__ dfc cscl(dfc a, df c) {
+  const float2 ch = splat(c.h);
+  const float2 p = pmul(a.h, ch);
+  float2 e = pfma(a.h, ch, p2(-p.x, -p.y));
+  e = pfma(a.h, splat(c.l), e);
+  e = pfma(a.l, ch, e);
+  return dnorm(p, e);
+}
+__device__ __forceinline__ dfc cconj(dfc a) { return dfc{p2(a.h.x, -a.h.y), p2(a.l.x, -a.l.y)}; }
+template <int SIGN>
+__device__ __forceinline__ dfc crot(dfc a) {
+  return SIGN < 0 ? dfc{p2(a.h.y, -a.h.x), p2(a.l.y, -a.l.x)} : dfc{p2(-a.h.y, a.h.x), p2(-a.l.y, a.l.x)};
+}
+
+// The generic names the stages use.
+template <typename T>
+__device__ __forceinline__ C2<T> add(C2<T> a, C2<T> b) { return cadd(a, b); }
+template <typename T>
+__device__ __forceinline__ C2<T> sub(C2<T> a, C2<T> b) { return csub(a, b); }
+template <typename T>
+__device__ __forceinline__ C2<T> mul(C2<T> a, C2<T> b) { return cmul(a, b); }
+template <typename T>
+__device__ __forceinline__ C2<T> scl(C2<T> a, T c) { return cscl(a, c); }
+template <typename T>
+__device__ __forceinline__ C2<T> conj(C2<T> a) { return cconj(a); }
+template <typename T, int SIGN>
+__device__ __forceinline__ C2<T> rot90(C2<T> a) { return crot<SIGN>(a); }
+// unnormalised sum / difference for double-float (FP64 and FP32 exact forms unaffected)
 template <typename T>
 __device__ __forceinline__ C2<T> addl(C2<T> a, C2<T> b) {
-  if constexpr (std::is_same<T, df>::value && DMG_DF_LAZY) {
-    return dfc{df_add_lazy(a.x, b.x), df_add_lazy(a.y, b.y)};
+  if constexpr (std::is_same<T, df>::value) {
+    return cadd_lazy(a, b);
   } else {
-    return add<T>(a, b);
+    return cadd(a, b);
   }
 }
 template <typename T>
 __device__ __forceinline__ C2<T> subl(C2<T> a, C2<T> b) {
-  if constexpr (std::is_same<T, df>::value && DMG_DF_LAZY) {
-    return dfc{df_add_lazy(a.x, -b.x), df_add_lazy(a.y, -b.y)};
+  if constexpr (std::is_same<T, df>::value) {
+    return csub_lazy(a, b);
   } else {
-    return sub<T>(a, b);
+    return csub(a, b);
   }
-}
-template <typename T>
-__device__ __forceinline__ C2<T> scl(C2<T> a, T s) { return mk<T>(a.x * s, a.y * s); }
-template <typename T>
-__device__ __forceinline__ C2<T> conj(C2<T> a) { return mk<T>(a.x, -a.y); }
-// multiply by sign*i
-template <typename T, int SIGN>
-__device__ __forceinline__ C2<T> rot90(C2<T> a) {
-  return SIGN < 0 ? mk<T>(a.y, -a.x) : mk<T>(-a.y, a.x);
 }
 
 // mathematical constants and their double-float splits
@@ -209,6 +266,8 @@ __device__ __forceinline__ C2<T> rot90(C2<T> a) {
 #define K_S144 0.587785252292473129168705954639072769, 0.5877852439880371f, 8.304436249773062e-09f
 #define K_HALF 0.5, 0.5f, 0.0f
 
+// Butterflies written with complex operations only (so that each maps to
+// paired instructions).
 template <typename T, int SIGN>
 __device__ __forceinline__ void dft4(C2<T> &a0, C2<T> &a1, C2<T> &a2, C2<T> &a3) {
   C2<T> t0 = addl<T>(a0, a2), t1 = subl<T>(a0, a2), t2 = addl<T>(a1, a3), t3 = rot90<T, SIGN>(subl<T>(a1, a3));
@@ -226,9 +285,9 @@ __device__ __forceinline__ void dft8(C2<T> *a) {
   dft4<T, SIGN>(o0, o1, o2, o3);
   const T c = cst<T>(K_SQRT1_2);
   // o1 *= (1 + sign i) c ; o2 *= sign i ; o3 *= (-1 + sign i) c
-  C2<T> w1 = SIGN < 0 ? mk<T>(c * (o1.x + o1.y), c * (o1.y - o1.x)) : mk<T>(c * (o1.x - o1.y), c * (o1.y + o1.x));
-  C2<T> w2 = rot90<T, SIGN>(o2);
-  C2<T> w3 = SIGN < 0 ? mk<T>(c * (o3.y - o3.x), -(c * (o3.x + o3.y))) : mk<T>(-(c * (o3.x + o3.y)), c * (o3.x - o3.y));
+  const C2<T> w1 = scl<T>(add<T>(o1, rot90<T, SIGN>(o1)), c);
+  const C2<T> w2 = rot90<T, SIGN>(o2);
+  const C2<T> w3 = scl<T>(sub<T>(rot90<T, SIGN>(o3), o3), c);
   a[0] = add<T>(e0, o0);
   a[4] = sub<T>(e0, o0);
   a[1] = add<T>(e1, w1);
@@ -241,11 +300,10 @@ __device__ __forceinline__ void dft8(C2<T> *a) {
 
 template <typename T, int SIGN>
 __device__ __forceinline__ void dft3(C2<T> *a) {
-  C2<T> s = add<T>(a[1], a[2]);
-  C2<T> d = sub<T>(a[1], a[2]);
-  const T half = cst<T>(K_HALF);
-  C2<T> m = mk<T>(a[0].x - half * s.x, a[0].y - half * s.y);
-  C2<T> r = rot90<T, SIGN>(scl<T>(d, cst<T>(K_SQRT3_2)));
+  const C2<T> s = add<T>(a[1], a[2]);
+  const C2<T> d = sub<T>(a[1], a[2]);
+  const C2<T> m = sub<T>(a[0], scl<T>(s, cst<T>(K_HALF)));
+  const C2<T> r = rot90<T, SIGN>(scl<T>(d, cst<T>(K_SQRT3_2)));
   a[0] = add<T>(a[0], s);
   a[1] = add<T>(m, r);
   a[2] = sub<T>(m, r);
@@ -253,18 +311,18 @@ __device__ __forceinline__ void dft3(C2<T> *a) {
 
 template <typename T, int SIGN>
 __device__ __forceinline__ void dft5(C2<T> *a) {
-  C2<T> b1 = add<T>(a[1], a[4]), b2 = add<T>(a[2], a[3]);
-  C2<T> d1 = sub<T>(a[1], a[4]), d2 = sub<T>(a[2], a[3]);
+  const C2<T> b1 = add<T>(a[1], a[4]), b2 = add<T>(a[2], a[3]);
+  const C2<T> d1 = sub<T>(a[1], a[4]), d2 = sub<T>(a[2], a[3]);
   const T c1 = cst<T>(K_C72), c2 = cst<T>(K_C144), s1 = cst<T>(K_S72), s2 = cst<T>(K_S144);
-  C2<T> p1 = mk<T>(a[0].x + c1 * b1.x + c2 * b2.x, a[0].y + c1 * b1.y + c2 * b2.y);
-  C2<T> p2 = mk<T>(a[0].x + c2 * b1.x + c1 * b2.x, a[0].y + c2 * b1.y + c1 * b2.y);
-  C2<T> q1 = rot90<T, SIGN>(mk<T>(s1 * d1.x + s2 * d2.x, s1 * d1.y + s2 * d2.y));
-  C2<T> q2 = rot90<T, SIGN>(mk<T>(s2 * d1.x - s1 * d2.x, s2 * d1.y - s1 * d2.y));
+  const C2<T> p1 = add<T>(a[0], add<T>(scl<T>(b1, c1), scl<T>(b2, c2)));
+  const C2<T> p2_ = add<T>(a[0], add<T>(scl<T>(b1, c2), scl<T>(b2, c1)));
+  const C2<T> q1 = rot90<T, SIGN>(add<T>(scl<T>(d1, s1), scl<T>(d2, s2)));
+  const C2<T> q2 = rot90<T, SIGN>(sub<T>(scl<T>(d1, s2), scl<T>(d2, s1)));
   a[0] = add<T>(a[0], add<T>(b1, b2));
   a[1] = add<T>(p1, q1);
   a[4] = sub<T>(p1, q1);
-  a[2] = add<T>(p2, q2);
-  a[3] = sub<T>(p2, q2);
+  a[2] = add<T>(p2_, q2);
+  a[3] = sub<T>(p2_, q2);
 }
 
 // ---------------------------------------------------------------- complex128 <-> double-float
@@ -428,8 +486,8 @@ __device__ __forceinline__ C2<T> root_at(const C2<T> *roots, int i) {
   C2<T> w;
   if constexpr (std::is_same<T, df>::value) {
     const float4 v = __ldg(reinterpret_cast<const float4 *>(roots) + i);
-    w.x = df{v.x, v.y};
-    w.y = df{v.z, v.w};
+    w.h = make_float2(v.x, v.y);
+    w.l = make_float2(v.z, v.w);
   } else {
     w = __ldg(roots + i);
   }
@@ -622,10 +680,8 @@ __device__ __forceinline__ C2<T> load_elem(const void *src, int64_t a, bool fp64
   if constexpr (std::is_same<T, df>::value) {
     if (fp64) {
       const double2 d = reinterpret_cast<const double2 *>(src)[a];
-      dfc r;
-      r.x = to_df(d.x, s);
-      r.y = to_df(d.y, s);
-      return r;
+      const df re = to_df(d.x, s), im = to_df(d.y, s);
+      return dfc{make_float2(re.h, im.h), make_float2(re.l, im.l)};
     }
   }
   (void)fp64;
@@ -638,8 +694,8 @@ __device__ __forceinline__ void store_elem(void *dst, int64_t a, C2<T> v, bool f
   if constexpr (std::is_same<T, df>::value) {
     if (fp64) {
       double2 d;
-      d.x = from_df(v.x, s);
-      d.y = from_df(v.y, s);
+      d.x = from_df(df{v.h.x, v.l.x}, s);
+      d.y = from_df(df{v.h.y, v.l.y}, s);
       reinterpret_cast<double2 *>(dst)[a] = d;
       return;
     }
@@ -988,8 +1044,8 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
         if constexpr (std::is_same<T, df>::value) {
           if (kc.in64) {
             const double2 d = *reinterpret_cast<const double2 *>(stg + sp);
-            v.x = to_df(d.x, sexp);
-            v.y = to_df(d.y, sexp);
+            const df re = to_df(d.x, sexp), im = to_df(d.y, sexp);
+            v = dfc{make_float2(re.h, im.h), make_float2(re.l, im.l)};
           } else {
             v = stg[sp];
           }
