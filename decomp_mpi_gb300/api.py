@@ -522,6 +522,33 @@ def read_file(path: str, decomp: "Decomp", elem_size: int, dst_ptr: int, stream=
                                   ctypes.c_void_p(stream)), "dmg_io_read_file")
 
 
+# ---------------------------------------------------------------- device visitors
+
+def decomp_scale(decomp: "Decomp", complex64: bool, data_ptr: int, factors, sign: int = -1, stream=None):
+    """dmg_decomp_scale: data *= prod_d factors[d][x_d] (conjugated for sign == 1); factors[d] a complex numpy
+    array of length L_d (complex128, or complex64 when complex64) or None."""
+    import numpy as np
+    keep = []
+    arr = (ctypes.c_void_p * 3)()
+    for d in range(3):
+        f = factors[d] if factors is not None and d < len(factors) else None
+        if f is not None:
+            f = np.ascontiguousarray(f, dtype=np.complex64 if complex64 else np.complex128)
+            keep.append(f)
+            arr[d] = f.ctypes.data
+        else:
+            arr[d] = None
+    check(load().dmg_decomp_scale(decomp.h, int(bool(complex64)), ctypes.c_void_p(data_ptr), arr, int(sign),
+                                  ctypes.c_void_p(stream)), "dmg_decomp_scale")
+    del keep
+
+
+def fill_index(decomp: "Decomp", type_size: int, data_ptr: int, stream=None):
+    """dmg_visit_fill_index: every held slot = its global C-order linear index."""
+    check(load().dmg_visit_fill_index(decomp.h, int(type_size), ctypes.c_void_p(data_ptr), ctypes.c_void_p(stream)),
+          "dmg_visit_fill_index")
+
+
 # ---------------------------------------------------------------- request server
 
 class _JobDesc(ctypes.Structure):
