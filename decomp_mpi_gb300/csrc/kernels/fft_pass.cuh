@@ -630,9 +630,12 @@ __host__ __device__ constexpr int fixed_radix(int nf, int lp) {
 
 // The Stockham stage after the first LP points of NF, from `in` to `out`.
 // roots: the pass's global table.
+// conv (first stage of a double-float pass that reads complex128): the
+// staging buffer holds raw complex128 values, converted here with the scale
+// exponent sexp as they are loaded.
 template <typename T, int SIGN, int NF, int LP>
 __device__ __forceinline__ void stage_fixed(const C2<T> *in, C2<T> *out, const C2<T> *roots, int nlines, int ld,
-                                            int tid) {
+                                            int tid, bool conv = false, int sexp = 0) {
   constexpr int R = fixed_radix(NF, LP);
   constexpr int NR = NF / R;
   constexpr int M = NR / LP;
@@ -647,7 +650,21 @@ __device__ __forceinline__ void stage_fixed(const C2<T> *in, C2<T> *out, const C
     C2<T> a[R];
 #pragma unroll
     for (int q = 0; q < R; ++q) {
-      C2<T> v = in[lo + swz<T, NF>(j * R * M + q * M + k)];
+      const int pos = lo + swz<T, NF>(j * R * M + q * M + k);
+      C2<T> v;
+      if constexpr (std::is_same<T, df>::value && LP == 1) {
+        if (conv) {
+          const double2 d = reinterpret_cast<const double2 *>(in)[pos];
+          const df re = to_df(d.x, sexp), im = to_df(d.y, sexp);
+          v = dfc{make_float2(re.h, im.h), make_float2(re.l, im.l)};
+        } else {
+          v = in[pos];
+        }
+      } else {
+        (void)conv;
+        (void)sexp;
+        v = in[pos];
+      }
       if (LP > 1 && q > 0) v = mul<T>(v, root_at<T, SIGN>(roots, j * q * TSTEP));
       a[q] = v;
     }
@@ -1025,8 +1042,11 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
     // ---- the tile's values are in the staging buffer ----
     copy_async_wait_all();
     __syncthreads();
-    // convert a complex128 input to double-float, apply the inverse split twiddle
-    if ((std::is_same<T, df>::value && kc.in64) || p.twiddle == 2) {
+    // convert a complex128 input to double-float, apply the inverse split
+    // twiddle (the compile-time-length kernels convert inside their first
+    // stage unless a twiddle is due here as well)
+    const bool conv_first = FIXED && std::is_same<T, df>::value && kc.in64 && p.twiddle != 2;
+    if ((std::is_same<T, df>::value && kc.in64 && !conv_first) || p.twiddle == 2) {
       const int n = FIXED ? NF : p.n;
       const int ld = kc.ld, M1 = kc.M1;
       const TileState &st = kc.ts[cur];
@@ -1076,7 +1096,8 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
       const C2<T> *stg = reinterpret_cast<const C2<T> *>(sm);
       C2<T> *bufA = reinterpret_cast<C2<T> *>(sm + kc.buf_a);
       if constexpr (FIXED) {
-        stage_fixed<T, SIGN, NF, 1>(stg, bufA, reinterpret_cast<const C2<T> *>(p.roots), nlines, ld, tid);
+        stage_fixed<T, SIGN, NF, 1>(stg, bufA, reinterpret_cast<const C2<T> *>(p.roots), nlines, ld, tid, conv_first,
+                                    kc.ts[cur].sexp);
       } else {
         stage_runtime<T, SIGN>(p, 0, 1, stg, bufA, reinterpret_cast<const C2<T> *>(p.roots), nlines, ld, tid);
       }
