@@ -36,6 +36,28 @@ __global__ void __launch_bounds__(256) maxexp_kernel(const dmg_fft_layout lay, i
   if ((threadIdx.x & 31) == 0 && best > 0) atomicMax(out, best);
 }
 
+// The same over a separable layout, a block per row of the last dimension
+// at a time: the row's address part is formed once, the threads run along
+// the row (contiguous in the usual layouts).
+__global__ void __launch_bounds__(256) maxexp_rows_kernel(const dmg_fft_layout lay, int ndim, int L0, int L1, int L2,
+                                                          const double2 *__restrict__ src, int32_t *out) {
+  const int64_t rows = (int64_t)L0 * L1;
+  int best = 0;
+  for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+    const int x0 = (int)(r / L1), x1 = (int)(r - (int64_t)x0 * L1);
+    const int64_t base = lay.base + __ldg(lay.tab[0] + x0) + (ndim > 1 ? __ldg(lay.tab[1] + x1) : 0);
+    for (int x2 = threadIdx.x; x2 < L2; x2 += blockDim.x) {
+      const double2 v = src[base + (ndim > 2 ? __ldg(lay.tab[2] + x2) : 0)];
+      const int ea = (int)((__double_as_longlong(v.x) >> 52) & 0x7FF);
+      const int eb = (int)((__double_as_longlong(v.y) >> 52) & 0x7FF);
+      best = max(best, max(ea, eb));
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
+  if ((threadIdx.x & 31) == 0 && best > 0) atomicMax(out, best);
+}
+
 }  // namespace
 
 extern "C" size_t dmg_fft_pass_smem(const dmg_fft_pass *p, int dtype) {
@@ -74,7 +96,13 @@ extern "C" int dmg_fft_maxexp_launch(const dmg_fft_layout *lay, int ndim, const 
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  maxexp_kernel<<<nsm * 8, 256, 0, s>>>(*lay, ndim, L0, L1, L2, static_cast<const double2 *>(src), out);
+  if (!lay->ranked) {
+    const int64_t rows = (int64_t)L0 * L1;
+    const int64_t grid = rows < (int64_t)nsm * 8 ? rows : (int64_t)nsm * 8;
+    maxexp_rows_kernel<<<(unsigned)grid, 256, 0, s>>>(*lay, ndim, L0, L1, L2, static_cast<const double2 *>(src), out);
+  } else {
+    maxexp_kernel<<<nsm * 8, 256, 0, s>>>(*lay, ndim, L0, L1, L2, static_cast<const double2 *>(src), out);
+  }
   e = cudaGetLastError();
   if (e != cudaSuccess) return dmg_error(DMG_ERR_CUDA, "maxexp launch: %s", cudaGetErrorString(e));
   return DMG_OK;
