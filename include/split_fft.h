@@ -148,7 +148,7 @@ int dmg_split_get_arith(SplitPlan plan);
  * and stores them in slot order (one HBM round trip per dimension; needs
  * L_d <= 2048 for complex128, 4096 for complex64).  SPLIT: the reference's
  * two stages, a pass per factor of each dimension with the twiddle between.
- * AUTO (default): LINES when every L_d is at most 512 (complex128) or 1024
+ * AUTO (default): LINES when every L_d is at most 1024 (complex128) or 2048
  * (complex64), else SPLIT. */
 #define DMG_SCHEDULE_AUTO 0
 #define DMG_SCHEDULE_LINES 1

@@ -197,9 +197,9 @@ def test_double_float_zero_input(cuda):
 
 @pytest.mark.parametrize("dtype", [api.C128, api.C64], ids=["c128", "c64"])
 def test_long_dimension_schedules(dtype, cuda):
-    """1024-point dimensions: auto picks the split schedule for complex128 and lines for complex64; both
+    """2048-point dimensions: auto picks the split schedule for complex128 and lines for complex64; both
     schedules give the same slots."""
-    P, spec, shape = 4, "packed:block(1024,2)|block(48,2)", (1024, 48)
+    P, spec, shape = 4, "packed:block(2048,2)|block(24,2)", (2048, 24)
     tol = TOL_C128 if dtype == api.C128 else TOL_C64
     r = Run(P, spec, shape, cuda, dtype=dtype)
     assert r.plan.schedule == (api.SCHEDULE_SPLIT if dtype == api.C128 else api.SCHEDULE_LINES)
