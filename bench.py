@@ -713,6 +713,73 @@ def run_precision(args):
     print(json.dumps(line))
 
 
+def run_fft(args):
+    """Split FFT alone: forward and inverse timings (CUDA events, median of 5 after 2 warm-up runs) and per-pass
+    times at n^3 on an 8x8 grid in the factor_reverse decomposition of the headline chain, for the chosen
+    element type and every arithmetic and schedule that applies.  One JSON line."""
+    import torch
+
+    from decomp_mpi_gb300 import api
+
+    n = args.n
+    dt = api.C64 if args.dtype == "c64" else api.C128
+    dev = torch.device("cuda:0")
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    _, _, frv = specs(n)
+    comm = api.Comm(P)
+    D = api.decomp_from_spec(comm, frv)
+    tdt = torch.complex128 if dt == api.C128 else torch.complex64
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(1)
+    dat = torch.empty(P * D.extent(), dtype=tdt, device=dev)
+    dat.real.uniform_(-1, 1, generator=gen)
+    dat.imag.uniform_(-1, 1, generator=gen)
+    probe = api.SplitPlan(D, 1 << 20, 1 << 40, 1 << 21, dtype=dt)
+    length = 2 * probe.extent64
+    probe.free()
+    work = torch.empty(P * length, dtype=tdt, device=dev)
+    sp = api.SplitPlan(D, dat.data_ptr(), length, work.data_ptr(), dtype=dt)
+    scheds = {"lines": [api.SCHEDULE_LINES], "split": [api.SCHEDULE_SPLIT],
+              "both": [api.SCHEDULE_LINES, api.SCHEDULE_SPLIT]}[args.schedule]
+    ariths = [api.ARITH_DF, api.ARITH_FP64] if dt == api.C128 else [api.ARITH_FP32]
+    out = {}
+    for sched in scheds:
+        try:
+            sp.set_schedule(sched)
+        except Exception:
+            continue
+        for ar in ariths:
+            sp.set_arith(ar)
+            for _ in range(2):
+                sp.run(api.FFTW_FORWARD, sh)
+                sp.run(api.FFTW_BACKWARD, sh)
+            torch.cuda.synchronize()
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            f, b = [], []
+            for _ in range(5):
+                e[0].record(stream)
+                sp.run(api.FFTW_FORWARD, sh)
+                e[1].record(stream)
+                sp.run(api.FFTW_BACKWARD, sh)
+                e[2].record(stream)
+                torch.cuda.synchronize()
+                f.append(e[0].elapsed_time(e[1]))
+                b.append(e[1].elapsed_time(e[2]))
+            sp.set_timing(True)
+            sp.run(api.FFTW_FORWARD, sh)
+            torch.cuda.synchronize()
+            passes = sp.pass_times(api.FFTW_FORWARD)
+            sp.set_timing(False)
+            key = "%s/%s" % ("lines" if sched == api.SCHEDULE_LINES else "split",
+                             {api.ARITH_FP64: "fp64", api.ARITH_FP32: "fp32", api.ARITH_DF: "double-float"}[ar])
+            out[key] = {"forward_ms": round(statistics.median(f), 3), "inverse_ms": round(statistics.median(b), 3),
+                        "forward_pass_ms": [round(x, 3) for x in passes],
+                        "forward_gflops": round(flops_per_transform(n ** 3) / (statistics.median(f) * 1e-3) / 1e9, 1)}
+    print(json.dumps({"mode": "fft", "n": n, "dtype": args.dtype, "grid": "8x8 virtual",
+                      "decomposition": frv, **out}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--sweep", action="store_true", help="reshape bandwidth sweep (one JSON line per case)")
@@ -722,6 +789,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=N_SIDE, help="cube side (the headline workload is 512)")
+    ap.add_argument("--fft", action="store_true", help="split FFT alone at --n: per-arithmetic, per-schedule times")
+    ap.add_argument("--dtype", default="c128", choices=["c128", "c64"], help="with --fft: element type")
+    ap.add_argument("--schedule", default="both", choices=["lines", "split", "both"], help="with --fft")
     ap.add_argument("--serve", action="store_true", help="served form: Poisson stream of mixed-size jobs")
     ap.add_argument("--precision", action="store_true", help="precision form: 1024^3 complex64 with error")
     ap.add_argument("--jobs", type=int, default=200, help="with --serve: jobs in the stream")
@@ -738,6 +808,9 @@ def main():
         return  # one GPU per run in this build: extra ranks do no work
     if args.sweep:
         run_sweep(args)
+        return
+    if args.fft:
+        run_fft(args)
         return
     if args.serve:
         run_serve(args)

@@ -615,6 +615,23 @@ __device__ __forceinline__ int swz(int i) {
   }
 }
 
+// Roots of the compile-time-length stages: staged in shared memory when
+// DMG_FFT_SMEM_ROOTS is set (the kernel copies the pass's table at start;
+// shared loads wait less than L1 loads), else read through L1 from the
+// global table.
+#ifndef DMG_FFT_SMEM_ROOTS
+#define DMG_FFT_SMEM_ROOTS 1
+#endif
+template <typename T, int SIGN>
+__device__ __forceinline__ C2<T> root_fx(const C2<T> *roots, int i) {
+  if constexpr (DMG_FFT_SMEM_ROOTS) {
+    const C2<T> w = roots[i];
+    return SIGN > 0 ? conj<T>(w) : w;
+  } else {
+    return root_at<T, SIGN>(roots, i);
+  }
+}
+
 // radix of the stage after the first LP points of NF (2, 3, 5-smooth): 8s
 // while the power-of-two part allows (16 done as 4 x 4), then 4, 2, 3, 5
 __host__ __device__ constexpr int fixed_radix(int nf, int lp) {
@@ -665,7 +682,7 @@ __device__ __forceinline__ void stage_fixed(const C2<T> *in, C2<T> *out, const C
         (void)sexp;
         v = in[pos];
       }
-      if (LP > 1 && q > 0) v = mul<T>(v, root_at<T, SIGN>(roots, j * q * TSTEP));
+      if (LP > 1 && q > 0) v = mul<T>(v, root_fx<T, SIGN>(roots, j * q * TSTEP));
       a[q] = v;
     }
     bfly_fixed<T, SIGN, R>(a);
@@ -731,6 +748,7 @@ __device__ __forceinline__ void store_elem(void *dst, int64_t a, C2<T> v, bool f
 struct SmemLayout {
   int ld;             // line pitch in values (odd)
   size_t buf_a, buf_b; // byte offsets of the stage buffers (the staging buffer is at 0)
+  size_t roots_off;   // n roots of the compile-time-length stages (when staged in shared memory)
   size_t contrib_off; // separable address parts: gather then scatter side, 1 + M1 + M2 int64 each
   size_t perm_off;    // int16 slot -> line position
   size_t total;
@@ -752,8 +770,9 @@ __host__ __device__ inline SmemLayout smem_layout(const dmg_fft_pass &p, bool fi
   const size_t one = (size_t)p.M1 * p.M2 * s.ld * es;
   s.buf_a = one;
   s.buf_b = 2 * one;
-  size_t pos = (3 * one + 7) & ~(size_t)7;
-  (void)fixed;
+  size_t pos = (3 * one + 15) & ~(size_t)15;
+  s.roots_off = pos;
+  if (fixed && DMG_FFT_SMEM_ROOTS) pos += (size_t)n * es;
   s.contrib_off = pos;
   pos += (size_t)2 * (1 + p.M1 + p.M2) * sizeof(int64_t);
   s.perm_off = pos;
@@ -835,7 +854,7 @@ struct TileState {
 // the FFT stages.
 struct PassConsts {
   int ld, M1, d0, mult0, td, v1_ytd, v2_ytd, in64, out64;
-  unsigned buf_a, buf_b, contrib_off, perm_off;
+  unsigned buf_a, buf_b, roots_off, contrib_off, perm_off;
   TileState ts[2];  // the tile being transformed and the one being gathered
 };
 
@@ -1005,6 +1024,7 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
     kc.M1 = p.M1;
     kc.buf_a = (unsigned)S.buf_a;
     kc.buf_b = (unsigned)S.buf_b;
+    kc.roots_off = (unsigned)S.roots_off;
     kc.contrib_off = (unsigned)S.contrib_off;
     kc.perm_off = (unsigned)S.perm_off;
     // the transform axis's dimension and step (separable sides)
@@ -1022,6 +1042,11 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
   __syncthreads();
   {
     const int n = FIXED ? NF : p.n;
+    if constexpr (FIXED && DMG_FFT_SMEM_ROOTS) {
+      C2<T> *sr = reinterpret_cast<C2<T> *>(sm + kc.roots_off);
+      const C2<T> *gr = reinterpret_cast<const C2<T> *>(p.roots);
+      for (int i = tid; i < n; i += NT) sr[i] = gr[i];
+    }
     if (p.perm_in || p.perm_out) {
       int16_t *perm = reinterpret_cast<int16_t *>(sm + kc.perm_off);
       for (int i = tid; i < n; i += NT) perm[i] = (int16_t)(i / p.perm_a + p.perm_b * (i % p.perm_a));
@@ -1124,7 +1149,9 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
       C2<T> *bufA = reinterpret_cast<C2<T> *>(sm + kc.buf_a);
       C2<T> *bufB = reinterpret_cast<C2<T> *>(sm + kc.buf_b);
       if constexpr (FIXED) {
-        res = stages_fixed<T, SIGN, NF, fixed_radix(NF, 1)>(bufA, bufB, bufA, reinterpret_cast<const C2<T> *>(p.roots),
+        const C2<T> *rts = DMG_FFT_SMEM_ROOTS ? reinterpret_cast<const C2<T> *>(sm + kc.roots_off)
+                                              : reinterpret_cast<const C2<T> *>(p.roots);
+        res = stages_fixed<T, SIGN, NF, fixed_radix(NF, 1)>(bufA, bufB, bufA, rts,
                                                             nlines, ld, tid);
       } else {
         const C2<T> *groots = reinterpret_cast<const C2<T> *>(p.roots);
