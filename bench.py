@@ -9,6 +9,12 @@ factor_reverse decomposition.  Inputs are seeded uniform[-1,1) values
 resident in HBM (2 GiB per array, larger than the 129 MB L2, so no L2 flush
 is needed between steps).
 
+With ``--gpus N`` under ``torch.distributed.run`` every rank runs its own
+replica of the workload on its own GPU (the path does not shard across GPUs:
+the processor grid is virtual, inside one GPU's memory).  The timed region is
+bracketed by a barrier on every rank, its duration is the maximum over the
+ranks, and ``value`` counts the transforms of all replicas.
+
 Prints one JSON line.  ``value`` is GFLOP/s of the whole step (two 3D
 transforms at 5 N log2 N flops each, divided by the time of the full step,
 reshapes included); the reshape GB/s and the FFT-only GFLOP/s are reported
@@ -78,14 +84,15 @@ class ClockSampler:
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self):
+    def __init__(self, index=None):
         self.proc = None
         self.lines = []
+        self.index = index if index is not None else os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]
 
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
-                                          "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                                          "-i", self.index,
                                           "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
                                          text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
@@ -133,9 +140,13 @@ def run_gpu(args):
     import torch
 
     from decomp_mpi_gb300 import api
+    from decomp_mpi_gb300.replicas import Replicas
 
-    dev = torch.device("cuda:0")
+    # one replica of the whole workload per GPU (the path does not shard across GPUs)
+    reps = Replicas()
+    dev = torch.device("cuda:%d" % reps.local_rank)
     torch.cuda.set_device(dev)
+    reps.init("nccl")
     n = args.n
     blk, rotd, frv = specs(n)
     comm = api.Comm(P)
@@ -182,19 +193,21 @@ def run_gpu(args):
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-    clocks = ClockSampler()
+    clocks = ClockSampler(reps.gpu_index())
     clocks.start()
     time.sleep(0.4)
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
+    reps.barrier()
     torch.cuda.synchronize()
     t0.record(stream)
     for _ in range(args.steps):
         step()
     t1.record(stream)
     torch.cuda.synchronize()
-    total_ms = t0.elapsed_time(t1)
+    reps.barrier()
     clk = clocks.stop()
+    total_ms = reps.max([t0.elapsed_time(t1)])[0]  # the slowest replica sets the job's time
 
     # component times (a separate pass with events between the parts)
     res_ms, fwd_ms, inv_ms = [], [], []
@@ -266,7 +279,8 @@ def run_gpu(args):
 
     ms_per_step = total_ms / args.steps
     flops_step = 2 * flops_per_transform(n_total)
-    gflops = flops_step / (ms_per_step * 1e-3) / 1e9
+    W = reps.world
+    gflops = W * flops_step / (ms_per_step * 1e-3) / 1e9  # every replica's transforms in the slowest one's time
     reshape_bytes = r01.bytes_moved + r12.bytes_moved
     reshape_gbs = reshape_bytes / (statistics.median(res_ms) * 1e-3) / 1e9
     fft_ms = statistics.median(fwd_ms) + statistics.median(inv_ms)
@@ -279,14 +293,17 @@ def run_gpu(args):
     fp64_peak = api.load().dmg_probe_fma_tflops(0)
     pass_tflops = flops_per_transform(n_total) / len(pass_fwd) / (avg_pass_ms * 1e-3) / 1e12
 
-    # end to end through the C-ABI with host buffers: H2D input, the step, D2H result
+    # end to end through the C-ABI with host buffers: every step uploads its input from pinned host memory and
+    # reads its result (the inverse's output) back.  Serial: copy, step, copy on one stream.  Pipelined (the
+    # reported e2e): two device buffer sets; step k+1's upload and step k's download run on copy streams while
+    # the kernels of the neighbouring step run, with events ordering every reuse of a buffer.
     host_in = torch.empty(a0.numel(), dtype=torch.complex128, pin_memory=True)
     host_in.copy_(a0.cpu())
-    host_out = torch.empty(a2.numel(), dtype=torch.complex128, pin_memory=True)
+    host_out = [torch.empty(a2.numel(), dtype=torch.complex128, pin_memory=True) for _ in range(2)]
     for _ in range(2):
         a0.copy_(host_in, non_blocking=True)
         step()
-        host_out.copy_(a2, non_blocking=True)
+        host_out[0].copy_(a2, non_blocking=True)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -294,20 +311,80 @@ def run_gpu(args):
     for _ in range(args.steps):
         a0.copy_(host_in, non_blocking=True)
         step()
-        host_out.copy_(a2, non_blocking=True)
+        host_out[0].copy_(a2, non_blocking=True)
     e1.record(stream)
     torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / args.steps
-    e2e = {"value": round(flops_step / (e2e_ms * 1e-3) / 1e9, 2), "unit": "GFLOP/s",
-           "h2d_bytes_per_step": host_in.numel() * 16, "d2h_bytes_per_step": host_out.numel() * 16,
-           "ms_per_step": round(e2e_ms, 3)}
+    serial_ms = e0.elapsed_time(e1) / args.steps
 
+    sets = [(a0, a1, a2, work)] + [(torch.empty_like(a0), torch.empty_like(a1), torch.empty_like(a2),
+                                    torch.empty_like(work))]
+    up, down = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    ev_up = [torch.cuda.Event() for _ in range(2)]
+    ev_comp = [torch.cuda.Event() for _ in range(2)]
+    ev_down = [torch.cuda.Event() for _ in range(2)]
+
+    def step_on(k):
+        b0, b1, b2, w = sets[k % 2]
+        r01.run(b0.data_ptr(), b1.data_ptr(), sh)
+        r12.run(b1.data_ptr(), b2.data_ptr(), sh)
+        sp.set_buffers(b2.data_ptr(), w.data_ptr())
+        sp.run(api.FFTW_FORWARD, sh)
+        sp.run(api.FFTW_BACKWARD, sh)
+
+    def pipelined(nsteps, timed):
+        if timed:
+            e0.record(stream)
+        up.wait_stream(stream)
+        down.wait_stream(stream)
+        with torch.cuda.stream(up):
+            sets[0][0].copy_(host_in, non_blocking=True)
+        ev_up[0].record(up)
+        for k in range(nsteps):
+            s = k % 2
+            stream.wait_event(ev_up[s])
+            if k >= 2:
+                stream.wait_event(ev_down[s])  # step k-2's result has left this set
+            step_on(k)
+            ev_comp[s].record(stream)
+            if k + 1 < nsteps:
+                if k >= 1:
+                    up.wait_event(ev_comp[1 - s])  # step k-1 has consumed the other set's input
+                with torch.cuda.stream(up):
+                    sets[1 - s][0].copy_(host_in, non_blocking=True)
+                ev_up[1 - s].record(up)
+            down.wait_event(ev_comp[s])
+            with torch.cuda.stream(down):
+                host_out[s].copy_(sets[s][2], non_blocking=True)
+            ev_down[s].record(down)
+        stream.wait_stream(down)
+        stream.wait_stream(up)
+        if timed:
+            e1.record(stream)
+        torch.cuda.synchronize()
+
+    pipelined(3, False)
+    reps.barrier()
+    pipelined(args.steps, True)
+    reps.barrier()
+    e2e_ms, serial_ms = reps.max([e0.elapsed_time(e1) / args.steps, serial_ms])
+    sp.set_buffers(a2.data_ptr(), work.data_ptr())
+    del sets
+    e2e = {"value": round(W * flops_step / (e2e_ms * 1e-3) / 1e9, 2), "unit": "GFLOP/s",
+           "h2d_bytes_per_step": host_in.numel() * 16, "d2h_bytes_per_step": host_out[0].numel() * 16,
+           "ms_per_step": round(e2e_ms, 3),
+           "note": "pipelined: step k+1's upload and step k's download overlap the kernels of the steps beside them",
+           "serial_ms_per_step": round(serial_ms, 3),
+           "serial_value": round(W * flops_step / (serial_ms * 1e-3) / 1e9, 2)}
+
+    if not reps.leader:
+        reps.close()
+        return
     cpu = cpu_baseline(args, reps=1)
     line = {
         "metric": "3D FFT GFLOP/s (5 N log2 N per transform) + reshape GB/s",
         "value": round(gflops, 2),
         "unit": "GFLOP/s",
-        "n_gpus": 1,
+        "n_gpus": W,
         "steps": args.steps,
         "warmup": args.warmup,
         "ms_per_step": round(ms_per_step, 3),
@@ -320,7 +397,8 @@ def run_gpu(args):
         "data": "synthetic: uniform[-1,1) complex128, seed 1, resident in HBM",
         "config": {"workload": workload_name(n), "virtual_ranks": P, "dat_pitch": r12.dest_pitch,
                    "work_length_per_rank": length, "l2": "inputs (2 GiB) larger than L2, no flush",
-                   "parallelism": "8x8 virtual grid on one GPU"},
+                   "parallelism": ("8x8 virtual grid on one GPU" if W == 1 else
+                                   "8x8 virtual grid per GPU, %d independent replicas" % W)},
         "fft_gflops": round(fft_gflops, 2),
         "reshape_gbs": round(reshape_gbs, 1),
         "reshape_frac_of_hbm": round(reshape_gbs / peak, 4),
@@ -345,12 +423,13 @@ def run_gpu(args):
                                                  "peak is the in-library FMA probe"}},
         "e2e": e2e,
         "gpu_launches": (r01.launches + r12.launches + sp.launches(api.FFTW_FORWARD)
-                         + sp.launches(api.FFTW_BACKWARD)) * args.steps,
+                         + sp.launches(api.FFTW_BACKWARD)) * args.steps * W,
         "clocks": clk,
         "cpu_baseline": cpu,
         "plans": {"reshape": [r01.describe(), r12.describe()], "split": sp.describe()},
     }
     print(json.dumps(line))
+    reps.close()
 
 
 # ----------------------------------------------------------------------------- CPU arm (reference algorithm)
@@ -804,8 +883,11 @@ def main():
     if args.impl == "reference":
         run_reference(args)
         return
+    if not (args.sweep or args.fft or args.serve or args.precision):
+        run_gpu(args)  # every rank: one replica of the workload per GPU
+        return
     if int(os.environ.get("WORLD_SIZE", "1")) > 1 and int(os.environ.get("RANK", "0")) != 0:
-        return  # one GPU per run in this build: extra ranks do no work
+        return  # the study modes run on one GPU: extra ranks do no work
     if args.sweep:
         run_sweep(args)
         return
@@ -818,7 +900,6 @@ def main():
     if args.precision:
         run_precision(args)
         return
-    run_gpu(args)
 
 
 if __name__ == "__main__":
