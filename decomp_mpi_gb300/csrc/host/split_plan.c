@@ -533,6 +533,13 @@ static int impl_upload(struct dmg_split_impl *im) {
 }
 
 /* Forward and inverse pass lists of the split schedule. */
+/* A pass's tile axes fastest first in memory, as letters: t the transform
+ * axis, a and b the first and second vector axes. */
+static void axis_letters(const int32_t *order, char *out) {
+  for (int i = 0; i < 3; ++i) out[i] = order[i] == 0 ? 't' : (order[i] == 1 ? 'a' : 'b');
+  out[3] = 0;
+}
+
 static int build_passes_split(struct dmg_split_impl *im) {
   int nd = im->ndim;
   int subs[MAXPASS], stage[MAXPASS];
@@ -599,8 +606,13 @@ static int build_passes_split(struct dmg_split_impl *im) {
                      nd > 2 ? im->B[2] : 1, K);
   for (int k = 0; k < K && pos < (int)sizeof(im->desc) - 64; ++k) {
     const struct dmg_fft_pass *p = &im->fwd[k].p;
-    pos += snprintf(im->desc + pos, sizeof(im->desc) - pos, " [t=%d n=%d v1=%d x%d v2=%d x%d tiles=%lld%s]", p->t,
-                    p->n, p->v1, p->M1, p->v2, p->M2, (long long)p->ntiles, p->twiddle ? " tw" : "");
+    char lo[4], so[4];
+    axis_letters(p->load_order, lo);
+    axis_letters(p->store_order, so);
+    pos += snprintf(im->desc + pos, sizeof(im->desc) - pos,
+                    " [t=%d n=%d v1=%d x%d v2=%d x%d tiles=%lld%s in=%s%s out=%s%s]", p->t, p->n, p->v1, p->M1, p->v2,
+                    p->M2, (long long)p->ntiles, p->twiddle ? " tw" : "", lo, p->sep_in ? "" : "(ranked)", so,
+                    p->sep_out ? "" : "(ranked)");
   }
   return DMG_OK;
 }
@@ -673,9 +685,13 @@ static int build_passes_line(struct dmg_split_impl *im) {
                      nd > 2 ? im->B[2] : 1, K);
   for (int k = 0; k < K && pos < (int)sizeof(im->desc) - 64; ++k) {
     const struct dmg_fft_pass *p = &im->fwd[k].p;
-    pos += snprintf(im->desc + pos, sizeof(im->desc) - pos, " [d=%d n=%d v1=%d x%d v2=%d x%d tiles=%lld%s]",
-                    p->t / 2, p->n, p->v1 >= 0 ? p->v1 / 2 : -1, p->M1, p->v2 >= 0 ? p->v2 / 2 : -1, p->M2,
-                    (long long)p->ntiles, p->perm_out ? " slots" : "");
+    char lo[4], so[4];
+    axis_letters(p->load_order, lo);
+    axis_letters(p->store_order, so);
+    pos += snprintf(im->desc + pos, sizeof(im->desc) - pos,
+                    " [d=%d n=%d v1=%d x%d v2=%d x%d tiles=%lld%s in=%s%s out=%s%s]", p->t / 2, p->n,
+                    p->v1 >= 0 ? p->v1 / 2 : -1, p->M1, p->v2 >= 0 ? p->v2 / 2 : -1, p->M2, (long long)p->ntiles,
+                    p->perm_out ? " slots" : "", lo, p->sep_in ? "" : "(ranked)", so, p->sep_out ? "" : "(ranked)");
   }
   return DMG_OK;
 }

@@ -645,6 +645,137 @@ __host__ __device__ constexpr int fixed_radix(int nf, int lp) {
   return rem;
 }
 
+// ---- power-of-two lengths: stage buffers addressed by XOR constants ----
+//
+// Between two stages of a power-of-two length the tile is kept in a layout
+// of its own: value x = line * NF + i (the line-major tile index) sits at
+// g(x) = x ^ ((x >> A1) & (V - 1)) [^ ((x >> A2) & (V - 1))], V values per
+// 128 bytes, with A1 = log2 of the consuming stage's radix.  g is linear over
+// GF(2) and the stage's index splits into disjoint bit fields (a thread's
+// butterfly base, the radix digit q * M, the output digit s * NR), so every
+// position is g(base) ^ g(digit) with g(digit) a compile-time constant: one
+// XOR per value instead of the index arithmetic.  The bank model this was
+// chosen with (16 lanes x 8 bytes or 8 lanes x 16 bytes per shared-memory
+// wavefront) gives one wavefront per access for every stage of the
+// lengths 16 ... 2048; length 32 needs its own terms.  The staging buffer the
+// gather fills and the buffer the scatter reads keep the line-padded layout.
+__host__ __device__ constexpr bool pow2_length(int n) { return n >= 8 && n <= 2048 && (n & (n - 1)) == 0; }
+__host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n >> 1); }
+// bytes per stage buffer of a power-of-two length kernel: the largest tile
+// of the pass in the line-padded layout
+__host__ __device__ constexpr size_t pow2_stride(size_t es, int n) {
+  return ((size_t)(DMG_FFT_TILE_TARGET(es) / n) * (size_t)(n | 1) * es + 15) & ~(size_t)15;
+}
+template <typename T, int NF, int LPC>  // LPC: the consuming stage's LP
+struct HopSwz {
+  static constexpr int S = swz_shift<T>();
+  static constexpr int A1 = NF == 32 ? (S == 3 ? 3 : 1) : ilog2(fixed_radix(NF, LPC));
+  static constexpr int A2 = (NF == 32 && S == 4) ? 3 : 0;
+  __host__ __device__ static constexpr int g(int x) {
+    return x ^ ((x >> A1) & ((1 << S) - 1)) ^ (A2 ? ((x >> A2) & ((1 << S) - 1)) : 0);
+  }
+};
+// value at swizzled index gx ^ c (c a compile-time constant) of a stage buffer
+template <typename T>
+__device__ __forceinline__ const C2<T> &at_xor(const C2<T> *buf, int gxb, int cb) {
+  return *reinterpret_cast<const C2<T> *>(reinterpret_cast<const unsigned char *>(buf) + (gxb ^ cb));
+}
+template <typename T>
+__device__ __forceinline__ C2<T> &at_xor(C2<T> *buf, int gxb, int cb) {
+  return *reinterpret_cast<C2<T> *>(reinterpret_cast<unsigned char *>(buf) + (gxb ^ cb));
+}
+
+// Twiddles of the power-of-two stages, staged in shared memory once per
+// block: stage (LP, R) keeps w_{LP R}^{j q} (conjugated for the inverse) at
+// LP - 1 + (q - 1) LP + j, so that a thread's R - 1 twiddles sit at
+// compile-time offsets from its j and neighbouring threads read neighbouring
+// entries.  The stages' tables add up to NF - 1 entries (the first stage's
+// are ones and unused).
+template <typename T, int SIGN, int NF>
+__device__ __forceinline__ void pow2_twiddles(const C2<T> *roots, C2<T> *tws, int tid) {
+  for (int e = tid; e < NF - 1; e += NT) {
+    int lp = 1;
+#pragma unroll
+    for (int s = 0; s < 12; ++s) {
+      const int r = fixed_radix(NF, lp);
+      if (e + 1 < lp * r) break;
+      lp *= r;
+    }
+    const int r = fixed_radix(NF, lp);
+    const int e2 = e - (lp - 1);
+    const int q = e2 / lp + 1, j = e2 % lp;
+    const C2<T> w = roots[j * q * (NF / (lp * r))];
+    tws[e] = SIGN > 0 ? conj<T>(w) : w;
+  }
+}
+
+// The Stockham stage after the first LP points of a power-of-two NF: from
+// the line-padded staging layout (first stage) or the previous stage's
+// swizzled layout, to the next stage's swizzled layout or (last stage) the
+// line-padded layout the scatter reads.  tws: the tables above.
+template <typename T, int SIGN, int NF, int LP>
+__device__ __forceinline__ void stage_pow2(const C2<T> *in, C2<T> *out, const C2<T> *tws, int nlines, int ld, int tid,
+                                           bool conv, int sexp) {
+  constexpr int R = fixed_radix(NF, LP);
+  constexpr int NR = NF / R;
+  constexpr int M = NR / LP;
+  constexpr int LGNR = ilog2(NR), LGM = ilog2(M), LGNF = ilog2(NF);
+  constexpr int ES = (int)sizeof(C2<T>);
+  constexpr bool IN_SWZ = LP > 1, OUT_SWZ = LP * R < NF;
+  using Gin = HopSwz<T, NF, LP>;
+  using Gout = HopSwz<T, NF, (LP * R < NF ? LP * R : LP)>;
+  const C2<T> *tw = tws + (LP - 1);
+  const int nb = nlines * NR;
+  for (int b = tid; b < nb; b += NT) {
+    const int l = b >> LGNR;
+    const int bb = b & (NR - 1);
+    const int j = bb >> LGM;
+    const int k = bb & (M - 1);
+    C2<T> a[R];
+    if constexpr (IN_SWZ) {
+      const int gxb = Gin::g((l << LGNF) + j * R * M + k) * ES;
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        C2<T> v = at_xor<T>(in, gxb, Gin::g(q * M) * ES);
+        if (q > 0) v = mul<T>(v, tw[(q - 1) * LP + j]);
+        a[q] = v;
+      }
+    } else {
+      const int lo = l * ld;
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        const int pos = lo + swz<T, NF>(q * M + k);
+        C2<T> v;
+        if constexpr (std::is_same<T, df>::value) {
+          if (conv) {
+            const double2 d = reinterpret_cast<const double2 *>(in)[pos];
+            const df re = to_df(d.x, sexp), im = to_df(d.y, sexp);
+            v = dfc{make_float2(re.h, im.h), make_float2(re.l, im.l)};
+          } else {
+            v = in[pos];
+          }
+        } else {
+          (void)conv;
+          (void)sexp;
+          v = in[pos];
+        }
+        a[q] = v;
+      }
+    }
+    bfly_fixed<T, SIGN, R>(a);
+    if constexpr (OUT_SWZ) {
+      const int gyb = Gout::g((l << LGNF) + bb) * ES;
+#pragma unroll
+      for (int s = 0; s < R; ++s) at_xor<T>(out, gyb, Gout::g(s * NR) * ES) = a[s];
+    } else {
+      const int lo = l * ld;
+#pragma unroll
+      for (int s = 0; s < R; ++s) out[lo + swz<T, NF>(bb + s * NR)] = a[s];
+    }
+  }
+  __syncthreads();
+}
+
 // The Stockham stage after the first LP points of NF, from `in` to `out`.
 // roots: the pass's global table.
 // conv (first stage of a double-float pass that reads complex128): the
@@ -698,7 +829,11 @@ template <typename T, int SIGN, int NF, int LP>
 __device__ __forceinline__ C2<T> *stages_fixed(C2<T> *in, C2<T> *out, C2<T> *spare, const C2<T> *roots, int nlines,
                                                int ld, int tid) {
   if constexpr (LP < NF) {
-    stage_fixed<T, SIGN, NF, LP>(in, out, roots, nlines, ld, tid);
+    if constexpr (pow2_length(NF)) {
+      stage_pow2<T, SIGN, NF, LP>(in, out, roots, nlines, ld, tid, false, 0);
+    } else {
+      stage_fixed<T, SIGN, NF, LP>(in, out, roots, nlines, ld, tid);
+    }
     return stages_fixed<T, SIGN, NF, LP * fixed_radix(NF, LP)>(out, spare, out, roots, nlines, ld, tid);
   } else {
     (void)out;
@@ -767,12 +902,12 @@ __host__ __device__ inline SmemLayout smem_layout(const dmg_fft_pass &p, bool fi
   const size_t es = sizeof(C2<T>);
   const int n = p.n;
   s.ld = n | 1;
-  const size_t one = (size_t)p.M1 * p.M2 * s.ld * es;
+  const size_t one = fixed && pow2_length(n) ? pow2_stride(es, n) : (size_t)p.M1 * p.M2 * s.ld * es;
   s.buf_a = one;
   s.buf_b = 2 * one;
   size_t pos = (3 * one + 15) & ~(size_t)15;
   s.roots_off = pos;
-  if (fixed && DMG_FFT_SMEM_ROOTS) pos += (size_t)n * es;
+  if (fixed && (DMG_FFT_SMEM_ROOTS || pow2_length(n))) pos += (size_t)n * es;
   s.contrib_off = pos;
   pos += (size_t)2 * (1 + p.M1 + p.M2) * sizeof(int64_t);
   s.perm_off = pos;
@@ -929,10 +1064,19 @@ __device__ __forceinline__ bool sep_walk(const int32_t *order, int n, int lim1, 
       for (int r = tid / ef; r < rows; r += rstep)
         f(a1 + AP(km, r), s1 + SP(km, r), C(0, i_f, r, 0), C(1, i_f, r, 0), C(2, i_f, r, 0));
     } else {
-      for (int r = tid / ef; r < rows; r += rstep) {
-        const int i_m = r % em, i_s = r / em;
+      // rows r = tid / ef + k * rstep as (i_m, i_s) = (r % em, r / em), stepped without dividing
+      const int r0 = tid / ef;
+      int i_m = r0 % em, i_s = r0 / em;
+      const int dm = rstep % em, ds = rstep / em;
+      while (i_s < es) {
         f(af + AP(km, i_m) + AP(ks, i_s), sf + SP(km, i_m) + SP(ks, i_s), C(0, i_f, i_m, i_s), C(1, i_f, i_m, i_s),
           C(2, i_f, i_m, i_s));
+        i_m += dm;
+        i_s += ds;
+        if (i_m >= em) {
+          i_m -= em;
+          ++i_s;
+        }
       }
     }
     return true;
@@ -948,14 +1092,17 @@ __device__ __forceinline__ bool sep_walk(const int32_t *order, int n, int lim1, 
       sf[j] = SP(kf, i_f);
     }
   }
-  for (int r = 0; r < rows; ++r) {
-    const int i_m = r % em, i_s = r / em;
+  for (int i_m = 0, i_s = 0; i_s < es;) {
     const int64_t ar = AP(km, i_m) + AP(ks, i_s);
     const int sr = SP(km, i_m) + SP(ks, i_s);
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const int i_f = tid + j * NT;
       if (i_f < ef) f(af[j] + ar, sf[j] + sr, C(0, i_f, i_m, i_s), C(1, i_f, i_m, i_s), C(2, i_f, i_m, i_s));
+    }
+    if (++i_m == em) {
+      i_m = 0;
+      ++i_s;
     }
   }
   return true;
@@ -1014,6 +1161,9 @@ __device__ __forceinline__ void gather_async(const dmg_fft_pass &p, const PassCo
 template <typename T, int SIGN, int NF>
 __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p, const dmg_fft_batch bt) {
   constexpr bool FIXED = NF > 0;
+  // power-of-two lengths: buffers at compile-time offsets (staging, A, B, twiddle tables)
+  constexpr bool POW2 = pow2_length(NF);
+  constexpr size_t PSTRIDE = POW2 ? pow2_stride(sizeof(C2<T>), NF) : 0;
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ PassConsts kc;
   const int tid = threadIdx.x;
@@ -1042,7 +1192,10 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
   __syncthreads();
   {
     const int n = FIXED ? NF : p.n;
-    if constexpr (FIXED && DMG_FFT_SMEM_ROOTS) {
+    if constexpr (POW2) {
+      pow2_twiddles<T, SIGN, NF>(reinterpret_cast<const C2<T> *>(p.roots), reinterpret_cast<C2<T> *>(sm + 3 * PSTRIDE),
+                                 tid);
+    } else if constexpr (FIXED && DMG_FFT_SMEM_ROOTS) {
       C2<T> *sr = reinterpret_cast<C2<T> *>(sm + kc.roots_off);
       const C2<T> *gr = reinterpret_cast<const C2<T> *>(p.roots);
       for (int i = tid; i < n; i += NT) sr[i] = gr[i];
@@ -1119,8 +1272,11 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
       const int ld = kc.ld;
       const int nlines = p.M1 * p.M2;
       const C2<T> *stg = reinterpret_cast<const C2<T> *>(sm);
-      C2<T> *bufA = reinterpret_cast<C2<T> *>(sm + kc.buf_a);
-      if constexpr (FIXED) {
+      C2<T> *bufA = reinterpret_cast<C2<T> *>(sm + (POW2 ? PSTRIDE : kc.buf_a));
+      if constexpr (POW2) {
+        stage_pow2<T, SIGN, NF, 1>(stg, bufA, reinterpret_cast<const C2<T> *>(sm + 3 * PSTRIDE), nlines, ld, tid,
+                                   conv_first, kc.ts[cur].sexp);
+      } else if constexpr (FIXED) {
         stage_fixed<T, SIGN, NF, 1>(stg, bufA, reinterpret_cast<const C2<T> *>(p.roots), nlines, ld, tid, conv_first,
                                     kc.ts[cur].sexp);
       } else {
@@ -1146,11 +1302,12 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
     {
       const int ld = kc.ld;
       const int nlines = p.M1 * p.M2;
-      C2<T> *bufA = reinterpret_cast<C2<T> *>(sm + kc.buf_a);
-      C2<T> *bufB = reinterpret_cast<C2<T> *>(sm + kc.buf_b);
+      C2<T> *bufA = reinterpret_cast<C2<T> *>(sm + (POW2 ? PSTRIDE : kc.buf_a));
+      C2<T> *bufB = reinterpret_cast<C2<T> *>(sm + (POW2 ? 2 * PSTRIDE : kc.buf_b));
       if constexpr (FIXED) {
-        const C2<T> *rts = DMG_FFT_SMEM_ROOTS ? reinterpret_cast<const C2<T> *>(sm + kc.roots_off)
-                                              : reinterpret_cast<const C2<T> *>(p.roots);
+        const C2<T> *rts = POW2 ? reinterpret_cast<const C2<T> *>(sm + 3 * PSTRIDE)
+                           : DMG_FFT_SMEM_ROOTS ? reinterpret_cast<const C2<T> *>(sm + kc.roots_off)
+                                                : reinterpret_cast<const C2<T> *>(p.roots);
         res = stages_fixed<T, SIGN, NF, fixed_radix(NF, 1)>(bufA, bufB, bufA, rts,
                                                             nlines, ld, tid);
       } else {
@@ -1285,8 +1442,10 @@ int launch_sign(const dmg_fft_pass &p, const dmg_fft_batch &bt, cudaStream_t s) 
   }
 }
 
-// Launch one pass over a batch of jobs in arithmetic T (checked by the caller).
-template <typename T>
+// Launch one pass of direction SIGN (p.sign) over a batch of jobs in
+// arithmetic T (checked by the caller).  The two directions are compiled in
+// separate translation units.
+template <typename T, int SIGN>
 int launch_pass(const dmg_fft_pass &p, const dmg_fft_batch &bt, void *stream) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (bt.count < 1 || bt.count > DMG_FFT_MAXBATCH)
@@ -1298,7 +1457,7 @@ int launch_pass(const dmg_fft_pass &p, const dmg_fft_batch &bt, void *stream) {
     if (std::is_same<T, df>::value && (p.in_fp64 || p.out_fp64) && !bt.scale_exp[j])
       return dmg_error(DMG_ERR_ARG, "double-float pass without a scale exponent");
   }
-  return p.sign < 0 ? launch_sign<T, -1>(p, bt, s) : launch_sign<T, 1>(p, bt, s);
+  return launch_sign<T, SIGN>(p, bt, s);
 }
 
 template <typename T>
