@@ -876,6 +876,11 @@ __device__ __forceinline__ void store_elem(void *dst, int64_t a, C2<T> v, bool f
 
 // ---------------------------------------------------------------- shared memory
 
+// int64 entries of one side's separable address parts for a tile: unused,
+// M1 entries of v1's dimension, M2 of v2's, 3 of the dimensions no tile axis
+// covers
+__host__ __device__ inline int parts_len(const dmg_fft_pass &p) { return 4 + p.M1 + p.M2; }
+
 // Carve-up of a pass block's dynamic shared memory (host and device agree):
 // the staging buffer the gather copies the next tile into, two buffers the
 // stages go between, then small tables.  Roots are read from the pass's
@@ -884,7 +889,7 @@ struct SmemLayout {
   int ld;             // line pitch in values (odd)
   size_t buf_a, buf_b; // byte offsets of the stage buffers (the staging buffer is at 0)
   size_t roots_off;   // n roots of the compile-time-length stages (when staged in shared memory)
-  size_t contrib_off; // separable address parts: gather then scatter side, 1 + M1 + M2 int64 each
+  size_t contrib_off; // separable address parts (parts_len int64 each): gather side, then two scatter-side areas
   size_t perm_off;    // int16 slot -> line position
   size_t total;
 };
@@ -909,7 +914,7 @@ __host__ __device__ inline SmemLayout smem_layout(const dmg_fft_pass &p, bool fi
   s.roots_off = pos;
   if (fixed && (DMG_FFT_SMEM_ROOTS || pow2_length(n))) pos += (size_t)n * es;
   s.contrib_off = pos;
-  pos += (size_t)2 * (1 + p.M1 + p.M2) * sizeof(int64_t);
+  pos += (size_t)3 * parts_len(p) * sizeof(int64_t);
   s.perm_off = pos;
   if (p.perm_in || p.perm_out) pos += (size_t)n * sizeof(int16_t);
   s.total = (pos + 15) & ~(size_t)15;
@@ -921,33 +926,6 @@ __host__ __device__ inline bool use_fixed(const dmg_fft_pass &p) {
   return fixed_length(p.n);
 }
 
-// Per-tile parts of a separable side's address: part[0] = base + the tables
-// of every dimension no tile axis covers, part[1 + c] and part[1 + M1 + c]
-// the entries of the v1 and v2 dimensions.
-__device__ __forceinline__ void sep_tile_parts(const dmg_fft_layout &L, const dmg_fft_pass &p, const int *xb,
-                                               int lim1, int lim2, int tid, int64_t *part) {
-  const int M1 = p.M1;
-  const int nc = 1 + M1 + p.M2;
-  for (int i = tid; i < nc; i += NT) {
-    if (i == 0) {
-      int64_t a = L.base;
-#pragma unroll
-      for (int d = 0; d < DMG_FFT_MAXDIM; ++d)
-        if (d < p.ndim && d != p.kdim[0] && d != p.kdim[1] && d != p.kdim[2]) a += __ldg(L.tab[d] + xb[d]);
-      part[0] = a;
-    } else {
-      const int k = i <= M1 ? 1 : 2;
-      const int c = k == 1 ? i - 1 : i - 1 - M1;
-      const int d = p.kdim[k];
-      if (d >= 0 && c < (k == 1 ? lim1 : lim2)) {
-        const int x = xb[d] + (p.kisz[k] ? p.A[d] * c : c);
-        part[i] = __ldg(L.tab[d] + x);
-      } else {
-        part[i] = 0;
-      }
-    }
-  }
-}
 
 // ---------------------------------------------------------------- asynchronous copies
 
@@ -965,6 +943,44 @@ __device__ __forceinline__ void copy_async(void *smem, const void *gmem) {
 }
 __device__ __forceinline__ void copy_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void copy_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Start the copies of one side's separable address parts for a tile (table
+// entries, asynchronously; part has parts_len entries): part[1 + c] and
+// part[1 + M1 + c] the entries of the v1 and v2 dimensions (0 past the tile's
+// extent), part[1 + M1 + M2 + u] that of dimension u when no tile axis
+// covers it (else 0).  The side's address is then L.base + the last three +
+// the tables of the tile axes.
+__device__ __forceinline__ void sep_parts_async(const dmg_fft_layout &L, const dmg_fft_pass &p, const int *yb,
+                                                const int *zb, int lim1, int lim2, int tid, int64_t *part) {
+  const int M1 = p.M1;
+  const int E = 1 + M1 + p.M2;
+  for (int i = tid; i < E + 3; i += NT) {
+    if (i == 0) {
+      part[0] = 0;
+    } else if (i >= E) {
+      const int d = i - E;
+      if (d < p.ndim && d != p.kdim[0] && d != p.kdim[1] && d != p.kdim[2])
+        copy_async<8>(part + i, L.tab[d] + (yb[d] + p.A[d] * zb[d]));
+      else
+        part[i] = 0;
+    } else {
+      const int k = i <= M1 ? 1 : 2;
+      const int c = k == 1 ? i - 1 : i - 1 - M1;
+      const int d = p.kdim[k];
+      if (d >= 0 && c < (k == 1 ? lim1 : lim2)) {
+        const int x = yb[d] + p.A[d] * zb[d] + (p.kisz[k] ? p.A[d] * c : c);
+        copy_async<8>(part + i, L.tab[d] + x);
+      } else {
+        part[i] = 0;
+      }
+    }
+  }
+}
+// the base of a separable side's addresses in a tile (parts complete)
+__device__ __forceinline__ int64_t sep_base(const dmg_fft_layout &L, const dmg_fft_pass &p, const int64_t *part) {
+  const int E = 1 + p.M1 + p.M2;
+  return L.base + part[E] + part[E + 1] + part[E + 2];
+}
 
 // ---------------------------------------------------------------- the pass kernel
 
@@ -987,27 +1003,43 @@ struct TileState {
 // Values every phase needs.  They live in shared memory and each phase
 // reads them after a barrier, so that none of them holds a register through
 // the FFT stages.
+// The tile index as digits (v1 tile, v2 tile, the batch sub-axes, the job;
+// radices nt1, nt2, blen[], count): a block steps through its tiles by
+// adding the digits of the grid size, without dividing.
+constexpr int NDIG = 9;
 struct PassConsts {
   int ld, M1, d0, mult0, td, v1_ytd, v2_ytd, in64, out64;
   unsigned buf_a, buf_b, roots_off, contrib_off, perm_off;
-  TileState ts[2];  // the tile being transformed and the one being gathered
+  int ndig, rad[NDIG], inc[NDIG], dig[NDIG];
+  TileState ts[3];  // the tile being transformed, the one being gathered, the one after
 };
 
+__device__ __forceinline__ void tile_digits(const int *rad, int nd, int64_t t, int *dig) {
+  for (int i = 0; i < nd; ++i) {
+    dig[i] = (int)(t % rad[i]);
+    t /= rad[i];
+  }
+}
+__device__ __forceinline__ void digits_add(int *dig, const int *inc, const int *rad, int nd) {
+  int carry = 0;
+  for (int i = 0; i < nd; ++i) {
+    const int v = dig[i] + inc[i] + carry;
+    carry = v >= rad[i];
+    dig[i] = carry ? v - rad[i] : v;
+  }
+}
+
+// A tile's place from its digits.
 template <typename T>
-__device__ __forceinline__ void tile_state(const dmg_fft_pass &p, const dmg_fft_batch &bt, int64_t tile,
-                                           TileState &st) {
-  st.job = (int)(tile / p.ntiles);
+__device__ __forceinline__ void tile_state_digits(const dmg_fft_pass &p, const dmg_fft_batch &bt, const int *dig,
+                                                  TileState &st) {
+  const int i1 = dig[0], i2 = dig[1];
+  st.job = dig[2 + p.nbatch];
   // scale exponent of the double-float conversions (bias removed, inputs end below 2)
   st.sexp = (std::is_same<T, df>::value && (p.in_fp64 || p.out_fp64)) ? __ldg(bt.scale_exp[st.job]) - 1022 : 0;
-  int64_t t = tile - (int64_t)st.job * p.ntiles;
-  const int i1 = (int)(t % p.nt1);
-  t /= p.nt1;
-  const int i2 = (int)(t % p.nt2);
-  t /= p.nt2;
   int yb[DMG_FFT_MAXDIM] = {0, 0, 0}, zb[DMG_FFT_MAXDIM] = {0, 0, 0};
   for (int b = 0; b < p.nbatch; ++b) {
-    const int c = (int)(t % p.blen[b]);
-    t /= p.blen[b];
+    const int c = dig[2 + b];
     const int s = p.bsub[b];
     if (s & 1) zb[s >> 1] += c;
     else yb[s >> 1] += c;
@@ -1028,6 +1060,7 @@ __device__ __forceinline__ void tile_state(const dmg_fft_pass &p, const dmg_fft_
   st.lim1 = p.v1 >= 0 ? min(p.M1, p.nv1 - i1 * p.M1) : 1;
   st.lim2 = p.v2 >= 0 ? min(p.M2, p.nv2 - i2 * p.M2) : 1;
 }
+
 
 // Visits the values of a tile that thread `tid` owns on a separable side,
 // calling f(address, staging position, c0, c1, c2).  Warps run along the
@@ -1112,7 +1145,8 @@ __device__ __forceinline__ bool sep_walk(const int32_t *order, int n, int lim1, 
 // complex128 input of a double-float pass is converted once it is there).
 template <typename T, int NF>
 __device__ __forceinline__ void gather_async(const dmg_fft_pass &p, const PassConsts &kc, const TileState &st,
-                                             const unsigned char *sm, const dmg_fft_batch &bt, int tid) {
+                                             const unsigned char *sm, const int64_t *pin, const dmg_fft_batch &bt,
+                                             int tid) {
   constexpr bool FIXED = NF > 0;
   const int n = FIXED ? NF : p.n;
   const int ld = kc.ld, M1 = kc.M1;
@@ -1125,10 +1159,9 @@ __device__ __forceinline__ void gather_async(const dmg_fft_pass &p, const PassCo
   const int lim1 = st.lim1, lim2 = st.lim2;
   const int total = n * lim1 * lim2;
   const int d0 = kc.d0, mult0 = kc.mult0;
-  const int64_t *pin = reinterpret_cast<const int64_t *>(sm + kc.contrib_off);
   const int16_t *perm = reinterpret_cast<const int16_t *>(sm + kc.perm_off);
   const int64_t *tab0 = p.in.tab[d0] + (yb[d0] + p.A[d0] * zb[d0]);
-  const int64_t in0 = p.sep_in ? pin[0] : 0;
+  const int64_t in0 = p.sep_in ? sep_base(p.in, p, pin) : 0;
   C2<T> *stg = reinterpret_cast<C2<T> *>(const_cast<unsigned char *>(sm));
   const unsigned char *gsrc = static_cast<const unsigned char *>(bt.src[st.job]);
   if (p.sep_in &&
@@ -1187,9 +1220,25 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
     kc.v2_ytd = p.kdim[2] == td && !p.kisz[2];
     kc.in64 = p.in_fp64 != 0;
     kc.out64 = p.out_fp64 != 0;
-    if (blockIdx.x < ntiles_all) tile_state<T>(p, bt, blockIdx.x, kc.ts[0]);
+    // this block's first two tiles, and the digits of the stride between its tiles
+    const int nd = 3 + p.nbatch;
+    kc.ndig = nd;
+    kc.rad[0] = p.nt1;
+    kc.rad[1] = p.nt2;
+    for (int b = 0; b < p.nbatch; ++b) kc.rad[2 + b] = p.blen[b];
+    kc.rad[2 + p.nbatch] = bt.count;
+    tile_digits(kc.rad, nd, blockIdx.x, kc.dig);
+    tile_digits(kc.rad, nd, gridDim.x, kc.inc);
+    if (blockIdx.x < ntiles_all) {
+      tile_state_digits<T>(p, bt, kc.dig, kc.ts[0]);
+      digits_add(kc.dig, kc.inc, kc.rad, nd);
+      if (blockIdx.x + gridDim.x < ntiles_all) tile_state_digits<T>(p, bt, kc.dig, kc.ts[1]);
+    }
   }
   __syncthreads();
+  // separable address parts: gather side, two scatter-side areas (tiles alternate)
+  int64_t *const parts_in = reinterpret_cast<int64_t *>(sm + kc.contrib_off);
+  int64_t *const parts_out0 = parts_in + parts_len(p);
   {
     const int n = FIXED ? NF : p.n;
     if constexpr (POW2) {
@@ -1204,22 +1253,38 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
       int16_t *perm = reinterpret_cast<int16_t *>(sm + kc.perm_off);
       for (int i = tid; i < n; i += NT) perm[i] = (int16_t)(i / p.perm_a + p.perm_b * (i % p.perm_a));
     }
-    if (p.sep_in && blockIdx.x < ntiles_all) {
-      int xb[DMG_FFT_MAXDIM];
-#pragma unroll
-      for (int d = 0; d < DMG_FFT_MAXDIM; ++d) xb[d] = kc.ts[0].yb[d] + p.A[d] * kc.ts[0].zb[d];
-      sep_tile_parts(p.in, p, xb, kc.ts[0].lim1, kc.ts[0].lim2, tid, reinterpret_cast<int64_t *>(sm + kc.contrib_off));
+    if (blockIdx.x < ntiles_all) {
+      const TileState &st = kc.ts[0];
+      if (p.sep_in) sep_parts_async(p.in, p, st.yb, st.zb, st.lim1, st.lim2, tid, parts_in);
+      if (p.sep_out) sep_parts_async(p.out, p, st.yb, st.zb, st.lim1, st.lim2, tid, parts_out0);
+      copy_async_commit();
     }
   }
+  copy_async_wait_all();
   __syncthreads();
-  if (blockIdx.x < ntiles_all) gather_async<T, NF>(p, kc, kc.ts[0], sm, bt, tid);
+  if (blockIdx.x < ntiles_all) gather_async<T, NF>(p, kc, kc.ts[0], sm, parts_in, bt, tid);
 
-  int cur = 0;
-  for (int64_t tile = blockIdx.x; tile < ntiles_all; tile += gridDim.x, cur ^= 1) {
+  int it = 0;
+  for (int64_t tile = blockIdx.x; tile < ntiles_all; tile += gridDim.x, ++it) {
     const int64_t next = tile + gridDim.x;
+    const int cur = it % 3, nxt = (it + 1) % 3;  // state slots of this tile and the next
     // ---- the tile's values are in the staging buffer ----
     copy_async_wait_all();
     __syncthreads();
+    // the state of the tile after the next (read after later barriers)
+    if (tid == 0 && next + gridDim.x < ntiles_all) {
+      digits_add(kc.dig, kc.inc, kc.rad, kc.ndig);
+      tile_state_digits<T>(p, bt, kc.dig, kc.ts[(it + 2) % 3]);
+    }
+    // the next tile's address parts start loading: gather side, and the
+    // scatter side into the area this tile's scatter does not read
+    if (next < ntiles_all) {
+      const TileState &sn = kc.ts[nxt];
+      if (p.sep_in) sep_parts_async(p.in, p, sn.yb, sn.zb, sn.lim1, sn.lim2, tid, parts_in);
+      if (p.sep_out)
+        sep_parts_async(p.out, p, sn.yb, sn.zb, sn.lim1, sn.lim2, tid, parts_out0 + ((it + 1) & 1) * parts_len(p));
+      copy_async_commit();
+    }
     // convert a complex128 input to double-float, apply the inverse split
     // twiddle (the compile-time-length kernels convert inside their first
     // stage unless a twiddle is due here as well)
@@ -1258,14 +1323,6 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
       }
       __syncthreads();
     }
-    // separable parts of the scatter side of this tile
-    if (p.sep_out) {
-      int xb[DMG_FFT_MAXDIM];
-#pragma unroll
-      for (int d = 0; d < DMG_FFT_MAXDIM; ++d) xb[d] = kc.ts[cur].yb[d] + p.A[d] * kc.ts[cur].zb[d];
-      sep_tile_parts(p.out, p, xb, kc.ts[cur].lim1, kc.ts[cur].lim2, tid,
-                     reinterpret_cast<int64_t *>(sm + kc.contrib_off) + (1 + p.M1 + p.M2));
-    }
 
     // ---- first Stockham stage: staging buffer -> A; then the next tile's copies start ----
     {
@@ -1284,17 +1341,9 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
       }
     }
     if (next < ntiles_all) {
-      if (tid == 0) tile_state<T>(p, bt, next, kc.ts[cur ^ 1]);
+      copy_async_wait_all();  // the next tile's address parts
       __syncthreads();
-      if (p.sep_in) {
-        int xb[DMG_FFT_MAXDIM];
-#pragma unroll
-        for (int d = 0; d < DMG_FFT_MAXDIM; ++d) xb[d] = kc.ts[cur ^ 1].yb[d] + p.A[d] * kc.ts[cur ^ 1].zb[d];
-        sep_tile_parts(p.in, p, xb, kc.ts[cur ^ 1].lim1, kc.ts[cur ^ 1].lim2, tid,
-                       reinterpret_cast<int64_t *>(sm + kc.contrib_off));
-        __syncthreads();
-      }
-      gather_async<T, NF>(p, kc, kc.ts[cur ^ 1], sm, bt, tid);
+      gather_async<T, NF>(p, kc, kc.ts[nxt], sm, parts_in, bt, tid);
     }
 
     // ---- the other stages: between A and B ----
@@ -1339,10 +1388,10 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
       const int lim1 = st.lim1, lim2 = st.lim2;
       const int total = n * lim1 * lim2;
       const int d0 = kc.d0, mult0 = kc.mult0;
-      const int64_t *pout = reinterpret_cast<const int64_t *>(sm + kc.contrib_off) + (1 + p.M1 + p.M2);
+      const int64_t *pout = parts_out0 + (it & 1) * parts_len(p);
       const int16_t *perm = reinterpret_cast<const int16_t *>(sm + kc.perm_off);
       const int64_t *tab0 = p.out.tab[d0] + (yb[d0] + p.A[d0] * zb[d0]);
-      const int64_t out0 = p.sep_out ? pout[0] : 0;
+      const int64_t out0 = p.sep_out ? sep_base(p.out, p, pout) : 0;
       const bool out64 = kc.out64;
       const int sexp = st.sexp;
       void *dst = bt.dst[st.job];
