@@ -890,7 +890,7 @@ struct SmemLayout {
   size_t buf_a, buf_b; // byte offsets of the stage buffers (the staging buffer is at 0)
   size_t roots_off;   // n roots of the compile-time-length stages (when staged in shared memory)
   size_t contrib_off; // separable address parts (parts_len int64 each): gather side, then two scatter-side areas
-  size_t perm_off;    // int16 slot -> line position
+  size_t perm_off;    // int16 buffer positions of the transform axis's coordinates: gather side, then scatter side
   size_t total;
 };
 
@@ -916,7 +916,7 @@ __host__ __device__ inline SmemLayout smem_layout(const dmg_fft_pass &p, bool fi
   s.contrib_off = pos;
   pos += (size_t)3 * parts_len(p) * sizeof(int64_t);
   s.perm_off = pos;
-  if (p.perm_in || p.perm_out) pos += (size_t)n * sizeof(int16_t);
+  pos += (size_t)2 * n * sizeof(int16_t);
   s.total = (pos + 15) & ~(size_t)15;
   return s;
 }
@@ -1071,15 +1071,111 @@ __device__ __forceinline__ void tile_state_digits(const dmg_fft_pass &p, const d
 // parts: the transform axis's from its table (tab0, step mult0), the vector
 // axes' from the per-tile table `part`.  Returns false (visiting nothing)
 // when the fast axis is longer than 8 * NT.
+// The same walk for the usual axis orders (ORD 0: t, v1, v2 fastest first;
+// 1: v1, t, v2; 2: v1, v2, t) with the axes' roles fixed at compile time, so
+// that a value costs its table reads and additions only.  Returns false
+// (visiting nothing) where it does not apply.
+__host__ __device__ constexpr int walk_order_code(int a, int b, int c) {
+  return (a == 0 && b == 1 && c == 2) ? 0 : (a == 1 && b == 0 && c == 2) ? 1 : (a == 1 && b == 2 && c == 0) ? 2 : -1;
+}
+template <typename T, int NF, int ORD, typename F>
+__device__ __forceinline__ bool sep_walk_ord(int n, int lim1, int lim2, int M1, int ld, const int64_t *tab0, int mult0,
+                                             int64_t base, const int64_t *part, const int16_t *spos, int tid, F &&f) {
+  const int nn = NF > 0 ? NF : n;
+  auto T0 = [&](int i) -> int64_t { return __ldg(tab0 + i * mult0); };
+  if constexpr (ORD == 0) {
+    if constexpr (NF > 0 && NF >= NT && NF % NT == 0 && NF / NT <= 8) {
+      // each thread keeps NF / NT coordinates along t; rows are the tile's lines
+      constexpr int J = NF / NT;
+      int64_t af[J];
+      int sf[J];
+#pragma unroll
+      for (int j = 0; j < J; ++j) {
+        af[j] = base + T0(tid + j * NT);
+        sf[j] = spos[tid + j * NT];
+      }
+      for (int i_s = 0; i_s < lim2; ++i_s) {
+        const int64_t a2 = part[1 + M1 + i_s];
+        for (int i_m = 0; i_m < lim1; ++i_m) {
+          const int64_t ar = a2 + part[1 + i_m];
+          const int sr = (i_m + M1 * i_s) * ld;
+#pragma unroll
+          for (int j = 0; j < J; ++j) f(af[j] + ar, sf[j] + sr, tid + j * NT, i_m, i_s);
+        }
+      }
+      return true;
+    } else {
+      return false;
+    }
+  } else {
+    // v1 fastest: each thread keeps one v1 coordinate; rows run over the
+    // other two axes (t then v2 for ORD 1, v2 then t for ORD 2)
+    const int ef = lim1;
+    if (ef > NT) return false;
+    const int rstep = NT / ef;
+    if (tid >= rstep * ef) return true;
+    const int i_f = tid % ef;
+    const int r0 = tid / ef;
+    const int64_t af = base + part[1 + i_f];
+    const int sf = i_f * ld;
+    if constexpr (ORD == 1) {
+      if (nn % rstep == 0) {
+        // rows r0 + k rstep: t = r0 + k rstep for k < nn / rstep within each v2 row
+        const int kn = nn / rstep;
+        for (int i_s = 0; i_s < lim2; ++i_s) {
+          const int64_t a2 = af + part[1 + M1 + i_s];
+          const int s2 = sf + i_s * M1 * ld;
+#pragma unroll 4
+          for (int k = 0; k < kn; ++k) {
+            const int t = r0 + k * rstep;
+            f(a2 + T0(t), s2 + spos[t], t, i_f, i_s);
+          }
+        }
+      } else {
+        int t = r0 % nn, i_s = r0 / nn;
+        const int dm = rstep % nn, ds = rstep / nn;
+        while (i_s < lim2) {
+          f(af + T0(t) + part[1 + M1 + i_s], sf + spos[t] + i_s * M1 * ld, t, i_f, i_s);
+          t += dm;
+          i_s += ds;
+          if (t >= nn) {
+            t -= nn;
+            ++i_s;
+          }
+        }
+      }
+    } else {
+      // rows (v2, t): v2 = r % lim2, t = r / lim2
+      int i_m = r0 % lim2, t = r0 / lim2;
+      const int dm = rstep % lim2, ds = rstep / lim2;
+      while (t < nn) {
+        f(af + part[1 + M1 + i_m] + T0(t), sf + i_m * M1 * ld + spos[t], t, i_f, i_m);
+        i_m += dm;
+        t += ds;
+        if (i_m >= lim2) {
+          i_m -= lim2;
+          ++t;
+        }
+      }
+    }
+    return true;
+  }
+}
+// walk by the side's order: a specialised form where one applies
+template <typename T, int NF, typename F>
+__device__ __forceinline__ bool sep_walk_any(const int32_t *order, int n, int lim1, int lim2, int M1, int ld,
+                                             const int64_t *tab0, int mult0, int64_t base, const int64_t *part,
+                                             const int16_t *spos, int tid, F &&f);
+
 template <typename T, int NF, typename F>
 __device__ __forceinline__ bool sep_walk(const int32_t *order, int n, int lim1, int lim2, int M1, int ld,
                                          const int64_t *tab0, int mult0, int64_t base, const int64_t *part,
-                                         const int16_t *perm, bool use_perm, int tid, F &&f) {
+                                         const int16_t *spos, int tid, F &&f) {
   const int kf = order[0], km = order[1], ks = order[2];
   auto E = [&](int k) { return k == 0 ? n : (k == 1 ? lim1 : lim2); };
   auto AP = [&](int k, int i) -> int64_t { return k == 0 ? __ldg(tab0 + i * mult0) : part[k == 1 ? 1 + i : 1 + M1 + i]; };
   auto SP = [&](int k, int i) -> int {
-    return k == 0 ? swz<T, NF>(use_perm ? (int)perm[i] : i) : (k == 1 ? i * ld : i * M1 * ld);
+    return k == 0 ? (int)spos[i] : (k == 1 ? i * ld : i * M1 * ld);
   };
   auto C = [&](int k, int i_f, int i_m, int i_s) { return kf == k ? i_f : (km == k ? i_m : i_s); };
   const int ef = E(kf), em = E(km), es = E(ks);
@@ -1141,6 +1237,17 @@ __device__ __forceinline__ bool sep_walk(const int32_t *order, int n, int lim1, 
   return true;
 }
 
+template <typename T, int NF, typename F>
+__device__ __forceinline__ bool sep_walk_any(const int32_t *order, int n, int lim1, int lim2, int M1, int ld,
+                                             const int64_t *tab0, int mult0, int64_t base, const int64_t *part,
+                                             const int16_t *spos, int tid, F &&f) {
+  const int code = walk_order_code(order[0], order[1], order[2]);
+  if (code == 0 && sep_walk_ord<T, NF, 0>(n, lim1, lim2, M1, ld, tab0, mult0, base, part, spos, tid, f)) return true;
+  if (code == 1 && sep_walk_ord<T, NF, 1>(n, lim1, lim2, M1, ld, tab0, mult0, base, part, spos, tid, f)) return true;
+  if (code == 2 && sep_walk_ord<T, NF, 2>(n, lim1, lim2, M1, ld, tab0, mult0, base, part, spos, tid, f)) return true;
+  return sep_walk<T, NF>(order, n, lim1, lim2, M1, ld, tab0, mult0, base, part, spos, tid, f);
+}
+
 // Start the copies of a tile into the staging buffer (raw values: a
 // complex128 input of a double-float pass is converted once it is there).
 template <typename T, int NF>
@@ -1159,14 +1266,14 @@ __device__ __forceinline__ void gather_async(const dmg_fft_pass &p, const PassCo
   const int lim1 = st.lim1, lim2 = st.lim2;
   const int total = n * lim1 * lim2;
   const int d0 = kc.d0, mult0 = kc.mult0;
-  const int16_t *perm = reinterpret_cast<const int16_t *>(sm + kc.perm_off);
+  const int16_t *spos = reinterpret_cast<const int16_t *>(sm + kc.perm_off);
   const int64_t *tab0 = p.in.tab[d0] + (yb[d0] + p.A[d0] * zb[d0]);
   const int64_t in0 = p.sep_in ? sep_base(p.in, p, pin) : 0;
   C2<T> *stg = reinterpret_cast<C2<T> *>(const_cast<unsigned char *>(sm));
   const unsigned char *gsrc = static_cast<const unsigned char *>(bt.src[st.job]);
   if (p.sep_in &&
-      sep_walk<T, NF>(p.load_order, n, lim1, lim2, M1, ld, tab0, mult0, in0, pin, perm, p.perm_in != 0, tid,
-                      [&](int64_t ad, int sp, int, int, int) {
+      sep_walk_any<T, NF>(p.load_order, n, lim1, lim2, M1, ld, tab0, mult0, in0, pin, spos, tid,
+                          [&](int64_t ad, int sp, int, int, int) {
                         copy_async<sizeof(C2<T>)>(stg + sp, gsrc + ad * (int64_t)sizeof(C2<T>));
                       })) {
     copy_async_commit();
@@ -1183,8 +1290,7 @@ __device__ __forceinline__ void gather_async(const dmg_fft_pass &p, const PassCo
       element_x(p, yb, zb, c0, c1, c2, x);
       ad = layout_addr(p.in, p.ndim, x);
     }
-    const int i = p.perm_in ? perm[c0] : c0;
-    const int sp = (c1 + M1 * c2) * ld + swz<T, NF>(i);
+    const int sp = (c1 + M1 * c2) * ld + spos[c0];
     copy_async<sizeof(C2<T>)>(stg + sp, gsrc + ad * (int64_t)sizeof(C2<T>));
   }
   copy_async_commit();
@@ -1249,9 +1355,15 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
       const C2<T> *gr = reinterpret_cast<const C2<T> *>(p.roots);
       for (int i = tid; i < n; i += NT) sr[i] = gr[i];
     }
-    if (p.perm_in || p.perm_out) {
-      int16_t *perm = reinterpret_cast<int16_t *>(sm + kc.perm_off);
-      for (int i = tid; i < n; i += NT) perm[i] = (int16_t)(i / p.perm_a + p.perm_b * (i % p.perm_a));
+    {
+      // buffer position of transform coordinate i on each side: the line
+      // position of slot i where that side is in slot order, swizzled
+      int16_t *spos = reinterpret_cast<int16_t *>(sm + kc.perm_off);
+      for (int i = tid; i < n; i += NT) {
+        const int slot = (p.perm_in || p.perm_out) ? i / p.perm_a + p.perm_b * (i % p.perm_a) : i;
+        spos[i] = (int16_t)swz<T, NF>(p.perm_in ? slot : i);
+        spos[n + i] = (int16_t)swz<T, NF>(p.perm_out ? slot : i);
+      }
     }
     if (blockIdx.x < ntiles_all) {
       const TileState &st = kc.ts[0];
@@ -1389,7 +1501,7 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
       const int total = n * lim1 * lim2;
       const int d0 = kc.d0, mult0 = kc.mult0;
       const int64_t *pout = parts_out0 + (it & 1) * parts_len(p);
-      const int16_t *perm = reinterpret_cast<const int16_t *>(sm + kc.perm_off);
+      const int16_t *spos = reinterpret_cast<const int16_t *>(sm + kc.perm_off) + n;
       const int64_t *tab0 = p.out.tab[d0] + (yb[d0] + p.A[d0] * zb[d0]);
       const int64_t out0 = p.sep_out ? sep_base(p.out, p, pout) : 0;
       const bool out64 = kc.out64;
@@ -1399,8 +1511,8 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
       const bool tw1 = p.twiddle == 1;
       const int ytw = st.ytw, v1y = kc.v1_ytd, v2y = kc.v2_ytd;
       bool done = p.sep_out &&
-                  sep_walk<T, NF>(p.store_order, n, lim1, lim2, M1, ld, tab0, mult0, out0, pout, perm,
-                                  p.perm_out != 0, tid, [&](int64_t ad, int sp, int c0, int c1, int c2) {
+                  sep_walk_any<T, NF>(p.store_order, n, lim1, lim2, M1, ld, tab0, mult0, out0, pout, spos, tid,
+                                      [&](int64_t ad, int sp, int c0, int c1, int c2) {
                                     C2<T> x = res[sp];
                                     if (tw1) {
                                       const int ex = (ytw + (v1y ? c1 : 0) + (v2y ? c2 : 0)) * c0;
@@ -1418,8 +1530,7 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
           ok[u] = e0 + tid + u * NT < total;
           if (ok[u]) {
             const int c0 = w.coord(p.store_pos[0]), c1 = w.coord(p.store_pos[1]), c2 = w.coord(p.store_pos[2]);
-            const int i = p.perm_out ? perm[c0] : c0;
-            C2<T> x = res[(c1 + M1 * c2) * ld + swz<T, NF>(i)];
+            C2<T> x = res[(c1 + M1 * c2) * ld + spos[c0]];
             if (p.twiddle == 1) {
               const int ex = (st.ytw + (kc.v1_ytd ? c1 : 0) + (kc.v2_ytd ? c2 : 0)) * c0;
               if (ex) x = mul<T>(x, twt[ex]);
