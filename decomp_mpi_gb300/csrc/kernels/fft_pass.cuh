@@ -98,8 +98,9 @@ __device__ __forceinline__ df operator*(df a, df b) {
 // A double-float complex number: the leading parts (re, im) in one pair and
 // the trailing parts in another, so that the two-sum and product-error steps
 // of the real and imaginary parts run as paired instructions.  Stored in
-// shared memory and HBM in the same order (re.hi, im.hi, re.lo, im.lo).
-struct dfc {
+// shared memory and HBM in the same order (re.hi, im.hi, re.lo, im.lo),
+// 16-byte aligned so that a value moves with one 16-byte access.
+struct __align__(16) dfc {
   float2 h, l;
 };
 template <typename T>
@@ -268,26 +269,36 @@ __device__ __forceinline__ C2<T> subl(C2<T> a, C2<T> b) {
 
 // Butterflies written with complex operations only (so that each maps to
 // paired instructions).
-template <typename T, int SIGN>
+// LAZY: outputs left unnormalised (double-float), for callers that only add
+// them or scale them further
+template <typename T, int SIGN, bool LAZY = false>
 __device__ __forceinline__ void dft4(C2<T> &a0, C2<T> &a1, C2<T> &a2, C2<T> &a3) {
   C2<T> t0 = addl<T>(a0, a2), t1 = subl<T>(a0, a2), t2 = addl<T>(a1, a3), t3 = rot90<T, SIGN>(subl<T>(a1, a3));
-  a0 = add<T>(t0, t2);
-  a2 = sub<T>(t0, t2);
-  a1 = add<T>(t1, t3);
-  a3 = sub<T>(t1, t3);
+  if constexpr (LAZY) {
+    a0 = addl<T>(t0, t2);
+    a2 = subl<T>(t0, t2);
+    a1 = addl<T>(t1, t3);
+    a3 = subl<T>(t1, t3);
+  } else {
+    a0 = add<T>(t0, t2);
+    a2 = sub<T>(t0, t2);
+    a1 = add<T>(t1, t3);
+    a3 = sub<T>(t1, t3);
+  }
 }
 
 template <typename T, int SIGN>
 __device__ __forceinline__ void dft8(C2<T> *a) {
   C2<T> e0 = a[0], e1 = a[2], e2 = a[4], e3 = a[6];
   C2<T> o0 = a[1], o1 = a[3], o2 = a[5], o3 = a[7];
-  dft4<T, SIGN>(e0, e1, e2, e3);
-  dft4<T, SIGN>(o0, o1, o2, o3);
+  // the inner sums stay unnormalised (double-float): only the outputs are normalised
+  dft4<T, SIGN, true>(e0, e1, e2, e3);
+  dft4<T, SIGN, true>(o0, o1, o2, o3);
   const T c = cst<T>(K_SQRT1_2);
   // o1 *= (1 + sign i) c ; o2 *= sign i ; o3 *= (-1 + sign i) c
-  const C2<T> w1 = scl<T>(add<T>(o1, rot90<T, SIGN>(o1)), c);
+  const C2<T> w1 = scl<T>(addl<T>(o1, rot90<T, SIGN>(o1)), c);
   const C2<T> w2 = rot90<T, SIGN>(o2);
-  const C2<T> w3 = scl<T>(sub<T>(rot90<T, SIGN>(o3), o3), c);
+  const C2<T> w3 = scl<T>(subl<T>(rot90<T, SIGN>(o3), o3), c);
   a[0] = add<T>(e0, o0);
   a[4] = sub<T>(e0, o0);
   a[1] = add<T>(e1, w1);
