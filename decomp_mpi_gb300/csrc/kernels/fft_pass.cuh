@@ -379,8 +379,8 @@ __device__ __noinline__ double from_df_slow(df v, int s) {
 // FP32<->FP64 conversions at 1/64 of its FP32 rate).  A normal double's
 // 53-bit significand m splits exactly into its 24-bit rounding mh (the
 // float hi) and the remainder r = m - mh * 2^29 (|r| <= 2^28, converted to
-// the float lo); back, hi and lo rejoin as M = mh * 2^29 + round(lo scaled),
-// renormalised by at most one bit.  Values whose pair would leave FP32's
+// the float lo); back, lo rounded to the places of hi's double is added to
+// that double's bit pattern.  Values whose pair would leave FP32's
 // normal range, zeros, subnormals, infinities and NaNs take the FP64 path.
 __device__ __forceinline__ df to_df(double x, int s) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
@@ -403,27 +403,20 @@ __device__ __forceinline__ df to_df(double x, int s) {
 }
 
 __device__ __forceinline__ double from_df(df v, int s) {
+  // the double of hi (exponent rebiased, scaled by 2^s) plus lo counted in
+  // that double's last places: an integer r added to its bit pattern, which
+  // carries into the exponent by itself; just below a power of two (hi's
+  // significand all zeros, r < 0) the places are half as large, so 2r
   const unsigned hb = __float_as_uint(v.h);
   const int fe = (int)((hb >> 23) & 0xFF);
-  if (fe < 52 || fe == 0xFF) return from_df_slow(v, s);
-  const long long mh = (long long)((hb & 0x7FFFFFu) | 0x800000u);
-  // lo in units of 2^(fe - 179), signed relative to hi's sign; |lo| <= ulp(hi) keeps it in range
-  const float ls = v.l * __uint_as_float((unsigned)(306 - fe) << 23);
-  if (!(fabsf(ls) < 1073741824.0f)) return from_df_slow(v, s);  // lo far outside hi's last bit
-  const int r = __float2int_rn((hb >> 31) ? -ls : ls);
-  long long M = (mh << 29) + r;
-  int E = fe + 896 + s;
-  if (M >= (1ll << 53)) {
-    M >>= 1;
-    ++E;
-  } else if (M < (1ll << 52)) {
-    M <<= 1;
-    --E;
-  }
-  if (E < 1 || E > 2046 || M < (1ll << 52) || M >= (1ll << 53)) return from_df_slow(v, s);
-  const unsigned long long bits =
-      ((unsigned long long)(hb >> 31) << 63) | ((unsigned long long)E << 52) | ((unsigned long long)M & 0x000FFFFFFFFFFFFFull);
-  return __longlong_as_double((long long)bits);
+  const int E = fe + 896 + s;
+  const float ls = v.l * __uint_as_float(((unsigned)(306 - fe) << 23) | (hb & 0x80000000u));
+  if (fe < 52 || fe == 0xFF || E < 2 || E > 2046 || !(fabsf(ls) < 1073741824.0f)) return from_df_slow(v, s);
+  const int r = __float2int_rn(ls);
+  const unsigned mant = hb & 0x7FFFFFu;
+  const long long hi = (long long)(((unsigned long long)(hb >> 31) << 63) | ((unsigned long long)E << 52) |
+                                   ((unsigned long long)mant << 29));
+  return __longlong_as_double(hi + ((mant == 0 && r < 0) ? 2ll * r : (long long)r));
 }
 
 // ---------------------------------------------------------------- addressing
