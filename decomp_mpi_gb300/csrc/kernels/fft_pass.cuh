@@ -935,15 +935,19 @@ __host__ __device__ inline bool use_fixed(const dmg_fft_pass &p) {
 
 // global -> shared copy of one value that completes in the background
 // (cp.async, 16 bytes through L2 only, 8 bytes through L1)
+// (sa: a shared-window address)
 template <int BYTES>
-__device__ __forceinline__ void copy_async(void *smem, const void *gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+__device__ __forceinline__ void copy_async_sa(unsigned sa, const void *gmem) {
   if constexpr (BYTES == 16) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
   } else {
     static_assert(BYTES == 8, "8- or 16-byte values");
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
   }
+}
+template <int BYTES>
+__device__ __forceinline__ void copy_async(void *smem, const void *gmem) {
+  copy_async_sa<BYTES>((unsigned)__cvta_generic_to_shared(smem), gmem);
 }
 __device__ __forceinline__ void copy_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void copy_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
@@ -1273,12 +1277,13 @@ __device__ __forceinline__ void gather_async(const dmg_fft_pass &p, const PassCo
   const int16_t *spos = reinterpret_cast<const int16_t *>(sm + kc.perm_off);
   const int64_t *tab0 = p.in.tab[d0] + (yb[d0] + p.A[d0] * zb[d0]);
   const int64_t in0 = p.sep_in ? sep_base(p.in, p, pin) : 0;
-  C2<T> *stg = reinterpret_cast<C2<T> *>(const_cast<unsigned char *>(sm));
+  const unsigned sbase = (unsigned)__cvta_generic_to_shared(sm);  // the staging buffer
   const unsigned char *gsrc = static_cast<const unsigned char *>(bt.src[st.job]);
   if (p.sep_in &&
       sep_walk_any<T, NF>(p.load_order, n, lim1, lim2, M1, ld, tab0, mult0, in0, pin, spos, tid,
                           [&](int64_t ad, int sp, int, int, int) {
-                        copy_async<sizeof(C2<T>)>(stg + sp, gsrc + ad * (int64_t)sizeof(C2<T>));
+                        copy_async_sa<sizeof(C2<T>)>(sbase + (unsigned)(sp * (int)sizeof(C2<T>)),
+                                                     gsrc + ad * (int64_t)sizeof(C2<T>));
                       })) {
     copy_async_commit();
     return;
@@ -1295,7 +1300,7 @@ __device__ __forceinline__ void gather_async(const dmg_fft_pass &p, const PassCo
       ad = layout_addr(p.in, p.ndim, x);
     }
     const int sp = (c1 + M1 * c2) * ld + spos[c0];
-    copy_async<sizeof(C2<T>)>(stg + sp, gsrc + ad * (int64_t)sizeof(C2<T>));
+    copy_async_sa<sizeof(C2<T>)>(sbase + (unsigned)(sp * (int)sizeof(C2<T>)), gsrc + ad * (int64_t)sizeof(C2<T>));
   }
   copy_async_commit();
 }
