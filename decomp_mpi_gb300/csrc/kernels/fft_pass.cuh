@@ -383,23 +383,22 @@ __device__ __noinline__ double from_df_slow(df v, int s) {
 // that double's bit pattern.  Values whose pair would leave FP32's
 // normal range, zeros, subnormals, infinities and NaNs take the FP64 path.
 __device__ __forceinline__ df to_df(double x, int s) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const int E = (int)((b >> 52) & 0x7FF);
+  // in 32-bit halves: hi's 23 stored significand bits are the double's top
+  // 23, rounded by the next bit (added to hi's bit pattern, so that a carry
+  // moves into the exponent); the remaining 29 bits, less 2^29 when hi
+  // rounded up, are lo in units of 2^(fe - 179)
+  const unsigned hb = (unsigned)__double2hiint(x), lb = (unsigned)__double2loint(x);
+  const int E = (int)((hb >> 20) & 0x7FF);
   const int fe = E - s - 896;  // float biased exponent of hi before rounding
   if (E == 0 || E == 0x7FF || fe < 53 || fe > 253) return to_df_slow(x, s);
-  const unsigned long long m = (b & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull;
-  unsigned long long mh = (m + (1ull << 28)) >> 29;  // 24 bits, or 2^24 when rounding carried
-  const long long r = (long long)m - (long long)(mh << 29);
-  int feh = fe;
-  if (mh >> 24) {
-    mh >>= 1;
-    ++feh;
-  }
-  const unsigned sign = (unsigned)(b >> 63) << 31;
-  const float h = __uint_as_float(sign | ((unsigned)feh << 23) | ((unsigned)mh & 0x7FFFFFu));
-  // lo = r * 2^(fe - 179); fe >= 53 keeps the power of two normal
-  const float l = (float)(int)r * __uint_as_float((unsigned)(fe - 52) << 23);
-  return df{h, sign ? -l : l};
+  const unsigned top = ((hb & 0xFFFFFu) << 3) | (lb >> 29);
+  const unsigned rb = (lb >> 28) & 1u;
+  const int r = (int)(lb & 0x1FFFFFFFu) - (int)(rb << 29);
+  const unsigned sign = hb & 0x80000000u;
+  const float h = __uint_as_float((sign | ((unsigned)fe << 23) | top) + rb);
+  // fe >= 53 keeps the power of two normal
+  const float l = (float)r * __uint_as_float(((unsigned)(fe - 52) << 23) | sign);
+  return df{h, l};
 }
 
 __device__ __forceinline__ double from_df(df v, int s) {
