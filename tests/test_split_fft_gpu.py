@@ -123,6 +123,25 @@ def test_forward_and_inverse_fp32(P, spec, shape, schedule, cuda):
     assert _rel(g, r.glob) < TOL_C64
 
 
+@pytest.mark.parametrize("dtype", [api.C128, api.C64], ids=["c128", "c64"])
+@pytest.mark.parametrize("P,spec,shape", [
+    # long contiguous lines (256 and 512 points, each thread keeping its line coordinates) and
+    # passes whose walks run along the first vector axis
+    (16, "packed:block(16,4)|block(32,4)|local(256)", (16, 32, 256)),
+    (4, "packed:block(8,2)|frev(4,2,block(8,2))|local(512)", (8, 8, 512)),
+    (16, "packed:frev(16,16,block(256,4))|block(8,4)|local(64)", (256, 8, 64)),
+], ids=["16x32x256", "8x8x512", "256x8x64"])
+def test_long_lines(P, spec, shape, dtype, cuda):
+    r = Run(P, spec, shape, cuda, dtype=dtype, schedule=api.SCHEDULE_LINES)
+    tol = TOL_C128 if dtype == api.C128 else TOL_C64
+    got = r.forward().astype(np.complex128)
+    exp, mask = O.split_expected_output(P, spec, r.glob, r.wl)
+    assert _rel(got[mask], exp[mask]) < tol
+    back = r.inverse().astype(np.complex128)
+    g = O.gather_global(P, spec, back, r.dp, r.shape) / np.prod(r.shape)
+    assert _rel(g, r.glob) < tol
+
+
 def test_delta_input_known_answer(cuda):
     """fftw_bench.c's delta at the origin: the forward transform is all ones (fftw_bench.c:118-124)."""
     import torch
