@@ -1,5 +1,6 @@
 // Batched FFT pass with fused layout change (shared by the per-arithmetic
-// translation units fft_pass_f64.cu, fft_pass_f32.cu, fft_pass_df.cu).
+// and per-direction translation units fft_pass_{f64,f32,df}.cu and
+// fft_pass_{f64,f32,df}_inv.cu).
 //
 // One launch transforms every line along one axis and writes the result in
 // another layout.  A block owns tiles of n x M1 x M2 values, persistent over
@@ -9,22 +10,27 @@
 // stages between two other buffers; the scatter stores the result to the
 // output layout in the order contiguous there, optionally multiplied by a
 // split twiddle, and in the split FFT's slot order for whole-dimension
-// passes.
+// passes.  A block steps through its tiles by adding the digits of the grid
+// size to the tile index's mixed-radix digits, and the next tile's address
+// parts load asynchronously behind the current tile's first stage.
 //
 // Stockham stage with radix r, Lp = product of earlier radices, m = n/(Lp r):
 //   a_q = w_{Lp r}^{j q} * x[j r m + q m + k],  y[(j + s Lp) m + k] = sum_q a_q w_r^{q s}
 // (j < Lp, k < m); the result is in natural order after the last stage.
 // Lengths known at compile time (powers of two 8...2048, the 2,3,5-smooth
-// cube sides 48...480) have fixed radix schedules, index arithmetic folded
-// into shifts and multiplications, and line positions XOR-swizzled (i ^ ((i /
-// V) mod V), V values per 128 bytes) so that strided stage accesses hit
-// distinct banks; other lengths take radices 8, 4, 2, 3, 5, 7 and direct DFTs
-// of larger primes from the pass.  Roots come from the pass's L1-resident
-// global table.
+// cube sides 48...480) have fixed radix schedules.  The power-of-two ones
+// keep the tile between stages in per-hop XOR-swizzled layouts (one XOR per
+// access, bank-conflict free) and read twiddles from per-stage tables staged
+// in shared memory; the others swizzle line positions (i ^ ((i / V) mod V),
+// V values per 128 bytes) and read the pass's root table.  Other lengths
+// take radices 8, 4, 2, 3, 5, 7 and direct DFTs of larger primes from the
+// pass.  The staging buffer and the buffer the scatter reads are
+// line-padded (odd pitch) with swizzled line positions.
 //
 // Addresses: a side whose address is separable over the tile axes keeps,
 // per tile, the part of the two vector axes in shared memory and reads the
-// transform axis's part from its table; ranked layouts are evaluated per
+// transform axis's part from its table; the usual axis orders walk with the
+// axes' roles fixed at compile time.  Ranked layouts are evaluated per
 // value.  Values every phase needs live in shared memory and are re-read
 // after barriers, so none holds a register through the stages.
 //
