@@ -1157,6 +1157,15 @@ __device__ __forceinline__ bool sep_walk_ord(int n, int lim1, int lim2, int M1, 
           }
         }
       }
+    } else if (lim2 == 1 && nn % rstep == 0) {
+      // one v2 value: rows are t = r0 + k rstep
+      const int kn = nn / rstep;
+      const int64_t a2 = af + part[1 + M1];
+#pragma unroll 4
+      for (int k = 0; k < kn; ++k) {
+        const int t = r0 + k * rstep;
+        f(a2 + T0(t), sf + spos[t], t, i_f, 0);
+      }
     } else {
       // rows (v2, t): v2 = r % lim2, t = r / lim2
       int i_m = r0 % lim2, t = r0 / lim2;
