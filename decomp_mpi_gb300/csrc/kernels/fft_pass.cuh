@@ -1094,6 +1094,8 @@ __host__ __device__ constexpr int walk_order_code(int a, int b, int c) {
 template <typename T, int NF, int ORD, typename F>
 __device__ __forceinline__ bool sep_walk_ord(int n, int lim1, int lim2, int M1, int ld, const int64_t *tab0, int mult0,
                                              int64_t base, const int64_t *part, const int16_t *spos, int tid, F &&f) {
+  // table reads in flight per thread: 8-byte values can afford more registers
+  constexpr int WALK_UNROLL = sizeof(C2<T>) == 8 ? 8 : 4;
   const int nn = NF > 0 ? NF : n;
   auto T0 = [&](int i) -> int64_t { return __ldg(tab0 + i * mult0); };
   if constexpr (ORD == 0) {
@@ -1138,7 +1140,7 @@ __device__ __forceinline__ bool sep_walk_ord(int n, int lim1, int lim2, int M1, 
         for (int i_s = 0; i_s < lim2; ++i_s) {
           const int64_t a2 = af + part[1 + M1 + i_s];
           const int s2 = sf + i_s * M1 * ld;
-#pragma unroll 4
+#pragma unroll WALK_UNROLL
           for (int k = 0; k < kn; ++k) {
             const int t = r0 + k * rstep;
             f(a2 + T0(t), s2 + spos[t], t, i_f, i_s);
@@ -1161,7 +1163,7 @@ __device__ __forceinline__ bool sep_walk_ord(int n, int lim1, int lim2, int M1, 
       // one v2 value: rows are t = r0 + k rstep
       const int kn = nn / rstep;
       const int64_t a2 = af + part[1 + M1];
-#pragma unroll 4
+#pragma unroll WALK_UNROLL
       for (int k = 0; k < kn; ++k) {
         const int t = r0 + k * rstep;
         f(a2 + T0(t), sf + spos[t], t, i_f, 0);
