@@ -855,6 +855,32 @@ def run_fft(args):
             out[key] = {"forward_ms": round(statistics.median(f), 3), "inverse_ms": round(statistics.median(b), 3),
                         "forward_pass_ms": [round(x, 3) for x in passes],
                         "forward_gflops": round(flops_per_transform(n ** 3) / (statistics.median(f) * 1e-3) / 1e9, 1)}
+            if n <= 128:
+                # small transforms are launch-bound: the same forward + inverse replayed from a CUDA graph
+                # (the plan's tables are on the device after the runs above, so capture allocates nothing)
+                try:
+                    cap = torch.cuda.Stream(dev)
+                    cap.wait_stream(stream)
+                    g = torch.cuda.CUDAGraph()
+                    with torch.cuda.graph(g, stream=cap):
+                        hs = torch.cuda.current_stream(dev).cuda_stream
+                        sp.run(api.FFTW_FORWARD, hs)
+                        sp.run(api.FFTW_BACKWARD, hs)
+                    for _ in range(3):
+                        g.replay()
+                    torch.cuda.synchronize()
+                    gt = []
+                    for _ in range(20):
+                        e[0].record(stream)
+                        g.replay()
+                        e[1].record(stream)
+                        torch.cuda.synchronize()
+                        gt.append(e[0].elapsed_time(e[1]))
+                    out[key]["graph_forward_inverse_ms"] = round(statistics.median(gt), 4)
+                except RuntimeError as err:
+                    out[key]["graph_forward_inverse_ms"] = None
+                    out[key]["graph_error"] = str(err).splitlines()[0][:200]
+                out[key]["eager_forward_inverse_ms"] = round(statistics.median(f) + statistics.median(b), 4)
     print(json.dumps({"mode": "fft", "n": n, "dtype": args.dtype, "grid": "8x8 virtual",
                       "decomposition": frv, **out}))
 
