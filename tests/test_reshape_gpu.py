@@ -170,3 +170,34 @@ def test_sweep_256_cubed(kind, tdt, cuda):
         "frev": "packed:frev(16,16,block(%d,%d))|frev(32,8,block(%d,%d))|local(%d)" % (n, g, n, g, n),
     }[kind]
     _index_roundtrip(g * g, blk, other, (n, n, n), getattr(torch, tdt), cuda)
+
+
+def test_cuda_graph_replay(cuda):
+    """A reshape run captured into a CUDA graph (after a first run has put its tables on the device)
+    replays to the eager result; a second source buffer gives its own permutation."""
+    import torch
+    P = 16
+    comm = api.Comm(P)
+    S = api.decomp_from_spec(comm, "packed:block(32,4)|block(32,4)|local(32)")
+    D = api.decomp_from_spec(comm, "packed:rotate(3,block(32,4))|rotate(11,block(32,4))|local(32)")
+    plan = api.ReshapePlan(comm, 16, S, D)
+    rng = np.random.default_rng(5)
+    src = torch.from_numpy(rng.standard_normal(2 * P * plan.src_pitch)).view(torch.complex128).to(cuda)
+    want = torch.zeros(P * plan.dest_pitch, dtype=torch.complex128, device=cuda)
+    got = torch.zeros_like(want)
+    stream = torch.cuda.current_stream(cuda)
+    plan.run(src.data_ptr(), want.data_ptr(), stream.cuda_stream)
+    torch.cuda.synchronize()
+    cap = torch.cuda.Stream(cuda)
+    cap.wait_stream(stream)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=cap):
+        plan.run(src.data_ptr(), got.data_ptr(), torch.cuda.current_stream(cuda).cuda_stream)
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(got, want)
+    src.copy_(src * 2)
+    g.replay()
+    plan.run(src.data_ptr(), want.data_ptr(), stream.cuda_stream)
+    torch.cuda.synchronize()
+    assert torch.equal(got, want)
