@@ -892,14 +892,14 @@ __host__ __device__ inline int parts_len(const dmg_fft_pass &p) { return 4 + p.M
 
 // Carve-up of a pass block's dynamic shared memory (host and device agree):
 // the staging buffer the gather copies the next tile into, two buffers the
-// stages go between, then small tables.  Roots are read from the pass's
-// global table (L1-resident).
+// stages go between, then small tables (twiddles or roots, address parts,
+// buffer positions along the transform axis).
 struct SmemLayout {
   int ld;             // line pitch in values (odd)
   size_t buf_a, buf_b; // byte offsets of the stage buffers (the staging buffer is at 0)
-  size_t roots_off;   // n roots of the compile-time-length stages (when staged in shared memory)
+  size_t roots_off;   // compile-time lengths: the per-stage twiddle tables (powers of two) or the n roots
   size_t contrib_off; // separable address parts (parts_len int64 each): gather side, then two scatter-side areas
-  size_t perm_off;    // int16 buffer positions of the transform axis's coordinates: gather side, then scatter side
+  size_t spos_off;    // int16 buffer positions of the transform axis's coordinates: gather side, then scatter side
   size_t total;
 };
 
@@ -924,7 +924,7 @@ __host__ __device__ inline SmemLayout smem_layout(const dmg_fft_pass &p, bool fi
   if (fixed && (DMG_FFT_SMEM_ROOTS || pow2_length(n))) pos += (size_t)n * es;
   s.contrib_off = pos;
   pos += (size_t)3 * parts_len(p) * sizeof(int64_t);
-  s.perm_off = pos;
+  s.spos_off = pos;
   pos += (size_t)2 * n * sizeof(int16_t);
   s.total = (pos + 15) & ~(size_t)15;
   return s;
@@ -1022,7 +1022,7 @@ struct TileState {
 constexpr int NDIG = 9;
 struct PassConsts {
   int ld, M1, d0, mult0, td, v1_ytd, v2_ytd, in64, out64;
-  unsigned buf_a, buf_b, roots_off, contrib_off, perm_off;
+  unsigned buf_a, buf_b, roots_off, contrib_off, spos_off;
   int ndig, rad[NDIG], inc[NDIG], dig[NDIG];
   TileState ts[3];  // the tile being transformed, the one being gathered, the one after
 };
@@ -1290,7 +1290,7 @@ __device__ __forceinline__ void gather_async(const dmg_fft_pass &p, const PassCo
   const int lim1 = st.lim1, lim2 = st.lim2;
   const int total = n * lim1 * lim2;
   const int d0 = kc.d0, mult0 = kc.mult0;
-  const int16_t *spos = reinterpret_cast<const int16_t *>(sm + kc.perm_off);
+  const int16_t *spos = reinterpret_cast<const int16_t *>(sm + kc.spos_off);
   const int64_t *tab0 = p.in.tab[d0] + (yb[d0] + p.A[d0] * zb[d0]);
   const int64_t in0 = p.sep_in ? sep_base(p.in, p, pin) : 0;
   const unsigned sbase = (unsigned)__cvta_generic_to_shared(sm);  // the staging buffer
@@ -1340,7 +1340,7 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
     kc.buf_b = (unsigned)S.buf_b;
     kc.roots_off = (unsigned)S.roots_off;
     kc.contrib_off = (unsigned)S.contrib_off;
-    kc.perm_off = (unsigned)S.perm_off;
+    kc.spos_off = (unsigned)S.spos_off;
     // the transform axis's dimension and step (separable sides)
     kc.d0 = p.kdim[0];
     kc.mult0 = p.kisz[0] ? p.A[p.kdim[0]] : 1;
@@ -1383,7 +1383,7 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
     {
       // buffer position of transform coordinate i on each side: the line
       // position of slot i where that side is in slot order, swizzled
-      int16_t *spos = reinterpret_cast<int16_t *>(sm + kc.perm_off);
+      int16_t *spos = reinterpret_cast<int16_t *>(sm + kc.spos_off);
       for (int i = tid; i < n; i += NT) {
         const int slot = (p.perm_in || p.perm_out) ? i / p.perm_a + p.perm_b * (i % p.perm_a) : i;
         spos[i] = (int16_t)swz<T, NF>(p.perm_in ? slot : i);
@@ -1526,7 +1526,7 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
       const int total = n * lim1 * lim2;
       const int d0 = kc.d0, mult0 = kc.mult0;
       const int64_t *pout = parts_out0 + (it & 1) * parts_len(p);
-      const int16_t *spos = reinterpret_cast<const int16_t *>(sm + kc.perm_off) + n;
+      const int16_t *spos = reinterpret_cast<const int16_t *>(sm + kc.spos_off) + n;
       const int64_t *tab0 = p.out.tab[d0] + (yb[d0] + p.A[d0] * zb[d0]);
       const int64_t out0 = p.sep_out ? sep_base(p.out, p, pout) : 0;
       const bool out64 = kc.out64;
