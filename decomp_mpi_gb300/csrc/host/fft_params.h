@@ -75,6 +75,11 @@ struct dmg_fft_pass {
    * axes (layout not ranked and the tile axes in different dimensions): the
    * kernel tabulates f0, f1, f2 once per tile */
   int32_t sep_in, sep_out;
+  /* separable side whose transform-axis table is the same for every tile
+   * (no batch sub-axis in that dimension) and whose entries lie within
+   * 2^31 of the first: the kernel may keep them in shared memory as int32
+   * offsets from that entry */
+  int32_t t0_rel_in, t0_rel_out;
   struct dmg_fft_layout in, out;
 };
 

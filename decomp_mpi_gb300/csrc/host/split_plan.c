@@ -388,6 +388,22 @@ static void impl_free(struct dmg_split_impl *im) {
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+/* whether a separable side's transform-axis entries qualify for the
+ * kernel's int32 shared-memory copy (see dmg_fft_pass.t0_rel_in) */
+static int t0_rel32(const fft_layout *l, const struct dmg_fft_pass *p) {
+  if (l->ranked) return 0;
+  const int d0 = p->kdim[0];
+  for (int b = 0; b < p->nbatch; ++b)
+    if ((p->bsub[b] >> 1) == d0) return 0;
+  const int mult0 = p->kisz[0] ? p->A[d0] : 1;
+  const int64_t *t = l->tab[d0];
+  for (int i = 0; i < p->n; ++i) {
+    const int64_t v = t[(int64_t)i * mult0] - t[0];
+    if (v < INT32_MIN || v > INT32_MAX) return 0;
+  }
+  return 1;
+}
+
 static void fill_side(struct dmg_fft_layout *fl, const fft_layout *hl, int nd, int64_t base) {
   memset(fl, 0, sizeof(*fl));
   for (int d = 0; d < nd; ++d) {
@@ -514,6 +530,8 @@ static int impl_upload(struct dmg_split_impl *im) {
       list[k].p.scale_exp = im->d_scale;
       fill_side(&list[k].p.in, &im->lay[list[k].in_lay], nd, list[k].in_base);
       fill_side(&list[k].p.out, &im->lay[list[k].out_lay], nd, list[k].out_base);
+      list[k].p.t0_rel_in = list[k].p.sep_in && t0_rel32(&im->lay[list[k].in_lay], &list[k].p);
+      list[k].p.t0_rel_out = list[k].p.sep_out && t0_rel32(&im->lay[list[k].out_lay], &list[k].p);
       /* scratch variant: an upper-half side moves to the fixed array */
       pass_rec *sr = dir == 0 ? &im->fwd_s[k] : &im->inv_s[k];
       *sr = list[k];

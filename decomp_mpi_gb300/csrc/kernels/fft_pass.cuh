@@ -885,6 +885,11 @@ __device__ __forceinline__ void store_elem(void *dst, int64_t a, C2<T> v, bool f
 
 // ---------------------------------------------------------------- shared memory
 
+// the largest dynamic shared memory per block with which the shared
+// transform-axis offsets are kept: two blocks per SM (228 KB, 1 KB reserved
+// per block, the block's static shared memory)
+#define DMG_FFT_T0_SMEM_LIMIT 115200
+
 // int64 entries of one side's separable address parts for a tile: unused,
 // M1 entries of v1's dimension, M2 of v2's, 3 of the dimensions no tile axis
 // covers
@@ -900,6 +905,8 @@ struct SmemLayout {
   size_t roots_off;   // compile-time lengths: the per-stage twiddle tables (powers of two) or the n roots
   size_t contrib_off; // separable address parts (parts_len int64 each): gather side, then two scatter-side areas
   size_t spos_off;    // int16 buffer positions of the transform axis's coordinates: gather side, then scatter side
+  size_t t0_off;      // int32 transform-axis address offsets (gather side, then scatter side) when has_t0
+  int has_t0;
   size_t total;
 };
 
@@ -926,6 +933,12 @@ __host__ __device__ inline SmemLayout smem_layout(const dmg_fft_pass &p, bool fi
   pos += (size_t)3 * parts_len(p) * sizeof(int64_t);
   s.spos_off = pos;
   pos += (size_t)2 * n * sizeof(int16_t);
+  // the transform axis's address offsets in shared memory where a side
+  // qualifies and two blocks per SM still fit
+  pos = (pos + 15) & ~(size_t)15;
+  s.t0_off = pos;
+  s.has_t0 = (p.t0_rel_in || p.t0_rel_out) && pos + (size_t)2 * n * sizeof(int32_t) <= DMG_FFT_T0_SMEM_LIMIT;
+  if (s.has_t0) pos += (size_t)2 * n * sizeof(int32_t);
   s.total = (pos + 15) & ~(size_t)15;
   return s;
 }
@@ -1022,7 +1035,9 @@ struct TileState {
 constexpr int NDIG = 9;
 struct PassConsts {
   int ld, M1, d0, mult0, td, v1_ytd, v2_ytd, in64, out64;
-  unsigned buf_a, buf_b, roots_off, contrib_off, spos_off;
+  unsigned buf_a, buf_b, roots_off, contrib_off, spos_off, t0_off;
+  int t0_in, t0_out;              // the sides whose transform-axis offsets are in shared memory
+  int64_t t0base_in, t0base_out;  // their first entries
   int ndig, rad[NDIG], inc[NDIG], dig[NDIG];
   TileState ts[3];  // the tile being transformed, the one being gathered, the one after
 };
@@ -1091,13 +1106,22 @@ __device__ __forceinline__ void tile_state_digits(const dmg_fft_pass &p, const d
 __host__ __device__ constexpr int walk_order_code(int a, int b, int c) {
   return (a == 0 && b == 1 && c == 2) ? 0 : (a == 1 && b == 0 && c == 2) ? 1 : (a == 1 && b == 2 && c == 0) ? 2 : -1;
 }
-template <typename T, int NF, int ORD, typename F>
+// REL: the transform axis's entries come from shared memory (t0rel, offsets
+// from t0base) instead of the table.
+template <typename T, int NF, int ORD, bool REL, typename F>
 __device__ __forceinline__ bool sep_walk_ord(int n, int lim1, int lim2, int M1, int ld, const int64_t *tab0, int mult0,
-                                             int64_t base, const int64_t *part, const int16_t *spos, int tid, F &&f) {
+                                             int64_t base, const int64_t *part, const int16_t *spos, int tid, F &&f,
+                                             const int32_t *t0rel, int64_t t0base) {
   // table reads in flight per thread: 8-byte values can afford more registers
   constexpr int WALK_UNROLL = sizeof(C2<T>) == 8 ? 8 : 4;
   const int nn = NF > 0 ? NF : n;
-  auto T0 = [&](int i) -> int64_t { return __ldg(tab0 + i * mult0); };
+  auto T0 = [&](int i) -> int64_t {
+    if constexpr (REL) {
+      return t0base + t0rel[i];
+    } else {
+      return __ldg(tab0 + i * mult0);
+    }
+  };
   if constexpr (ORD == 0) {
     if constexpr (NF > 0 && NF >= NT && NF % NT == 0 && NF / NT <= 8) {
       // each thread keeps NF / NT coordinates along t; rows are the tile's lines
@@ -1189,7 +1213,8 @@ __device__ __forceinline__ bool sep_walk_ord(int n, int lim1, int lim2, int M1, 
 template <typename T, int NF, typename F>
 __device__ __forceinline__ bool sep_walk_any(const int32_t *order, int n, int lim1, int lim2, int M1, int ld,
                                              const int64_t *tab0, int mult0, int64_t base, const int64_t *part,
-                                             const int16_t *spos, int tid, F &&f);
+                                             const int16_t *spos, int tid, F &&f, const int32_t *t0rel,
+                                             int64_t t0base);
 
 template <typename T, int NF, typename F>
 __device__ __forceinline__ bool sep_walk(const int32_t *order, int n, int lim1, int lim2, int M1, int ld,
@@ -1264,11 +1289,24 @@ __device__ __forceinline__ bool sep_walk(const int32_t *order, int n, int lim1, 
 template <typename T, int NF, typename F>
 __device__ __forceinline__ bool sep_walk_any(const int32_t *order, int n, int lim1, int lim2, int M1, int ld,
                                              const int64_t *tab0, int mult0, int64_t base, const int64_t *part,
-                                             const int16_t *spos, int tid, F &&f) {
+                                             const int16_t *spos, int tid, F &&f, const int32_t *t0rel,
+                                             int64_t t0base) {
   const int code = walk_order_code(order[0], order[1], order[2]);
-  if (code == 0 && sep_walk_ord<T, NF, 0>(n, lim1, lim2, M1, ld, tab0, mult0, base, part, spos, tid, f)) return true;
-  if (code == 1 && sep_walk_ord<T, NF, 1>(n, lim1, lim2, M1, ld, tab0, mult0, base, part, spos, tid, f)) return true;
-  if (code == 2 && sep_walk_ord<T, NF, 2>(n, lim1, lim2, M1, ld, tab0, mult0, base, part, spos, tid, f)) return true;
+  if (code == 0 &&
+      sep_walk_ord<T, NF, 0, false>(n, lim1, lim2, M1, ld, tab0, mult0, base, part, spos, tid, f, t0rel, t0base))
+    return true;
+  if (code == 1 && t0rel &&
+      sep_walk_ord<T, NF, 1, true>(n, lim1, lim2, M1, ld, tab0, mult0, base, part, spos, tid, f, t0rel, t0base))
+    return true;
+  if (code == 1 && !t0rel &&
+      sep_walk_ord<T, NF, 1, false>(n, lim1, lim2, M1, ld, tab0, mult0, base, part, spos, tid, f, t0rel, t0base))
+    return true;
+  if (code == 2 && t0rel &&
+      sep_walk_ord<T, NF, 2, true>(n, lim1, lim2, M1, ld, tab0, mult0, base, part, spos, tid, f, t0rel, t0base))
+    return true;
+  if (code == 2 && !t0rel &&
+      sep_walk_ord<T, NF, 2, false>(n, lim1, lim2, M1, ld, tab0, mult0, base, part, spos, tid, f, t0rel, t0base))
+    return true;
   return sep_walk<T, NF>(order, n, lim1, lim2, M1, ld, tab0, mult0, base, part, spos, tid, f);
 }
 
@@ -1300,7 +1338,8 @@ __device__ __forceinline__ void gather_async(const dmg_fft_pass &p, const PassCo
                           [&](int64_t ad, int sp, int, int, int) {
                         copy_async_sa<sizeof(C2<T>)>(sbase + (unsigned)(sp * (int)sizeof(C2<T>)),
                                                      gsrc + ad * (int64_t)sizeof(C2<T>));
-                      })) {
+                      },
+                          kc.t0_in ? reinterpret_cast<const int32_t *>(sm + kc.t0_off) : nullptr, kc.t0base_in)) {
     copy_async_commit();
     return;
   }
@@ -1341,6 +1380,11 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
     kc.roots_off = (unsigned)S.roots_off;
     kc.contrib_off = (unsigned)S.contrib_off;
     kc.spos_off = (unsigned)S.spos_off;
+    kc.t0_off = (unsigned)S.t0_off;
+    kc.t0_in = S.has_t0 && p.t0_rel_in;
+    kc.t0_out = S.has_t0 && p.t0_rel_out;
+    kc.t0base_in = kc.t0_in ? __ldg(p.in.tab[p.kdim[0]]) : 0;
+    kc.t0base_out = kc.t0_out ? __ldg(p.out.tab[p.kdim[0]]) : 0;
     // the transform axis's dimension and step (separable sides)
     kc.d0 = p.kdim[0];
     kc.mult0 = p.kisz[0] ? p.A[p.kdim[0]] : 1;
@@ -1389,6 +1433,13 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
         spos[i] = (int16_t)swz<T, NF>(p.perm_in ? slot : i);
         spos[n + i] = (int16_t)swz<T, NF>(p.perm_out ? slot : i);
       }
+      // transform-axis address offsets (every tile's: no batch sub-axis in that dimension)
+      int32_t *t0 = reinterpret_cast<int32_t *>(sm + kc.t0_off);
+      const int d0 = p.kdim[0], m0 = kc.mult0;
+      if (kc.t0_in)
+        for (int i = tid; i < n; i += NT) t0[i] = (int32_t)(__ldg(p.in.tab[d0] + i * m0) - kc.t0base_in);
+      if (kc.t0_out)
+        for (int i = tid; i < n; i += NT) t0[n + i] = (int32_t)(__ldg(p.out.tab[d0] + i * m0) - kc.t0base_out);
     }
     if (blockIdx.x < ntiles_all) {
       const TileState &st = kc.ts[0];
@@ -1544,7 +1595,9 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
                                       if (ex) x = mul<T>(x, twt[ex]);
                                     }
                                     store_elem<T>(dst, ad, x, out64, sexp);
-                                  });
+                                  },
+                                  kc.t0_out ? reinterpret_cast<const int32_t *>(sm + kc.t0_off) + n : nullptr,
+                                  kc.t0base_out);
       TileWalk w(tid, p.store_pos, n, lim1, lim2);
       for (int e0 = 0; !done && e0 < total; e0 += NT * EPT) {
         int64_t ad[EPT];
