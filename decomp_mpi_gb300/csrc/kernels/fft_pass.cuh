@@ -886,9 +886,10 @@ __device__ __forceinline__ void store_elem(void *dst, int64_t a, C2<T> v, bool f
 // ---------------------------------------------------------------- shared memory
 
 // the largest dynamic shared memory per block with which the shared
-// transform-axis offsets are kept: two blocks per SM (228 KB, 1 KB reserved
-// per block, the block's static shared memory)
-#define DMG_FFT_T0_SMEM_LIMIT 115200
+// transform-axis offsets are kept: two blocks per SM, each at most 112 KB
+// with its 1 KB reserve and static shared memory (measured: at 115 KB the
+// 1024-point FP32 passes fell to one block per SM)
+#define DMG_FFT_T0_SMEM_LIMIT 113328
 
 // int64 entries of one side's separable address parts for a tile: unused,
 // M1 entries of v1's dimension, M2 of v2's, 3 of the dimensions no tile axis
@@ -905,8 +906,8 @@ struct SmemLayout {
   size_t roots_off;   // compile-time lengths: the per-stage twiddle tables (powers of two) or the n roots
   size_t contrib_off; // separable address parts (parts_len int64 each): gather side, then two scatter-side areas
   size_t spos_off;    // int16 buffer positions of the transform axis's coordinates: gather side, then scatter side
-  size_t t0_off;      // int32 transform-axis address offsets (gather side, then scatter side) when has_t0
-  int has_t0;
+  size_t t0_off;      // int32 transform-axis address offsets: gather side (has_t0_in), then scatter side (has_t0_out)
+  int has_t0_in, has_t0_out;
   size_t total;
 };
 
@@ -937,8 +938,10 @@ __host__ __device__ inline SmemLayout smem_layout(const dmg_fft_pass &p, bool fi
   // qualifies and two blocks per SM still fit
   pos = (pos + 15) & ~(size_t)15;
   s.t0_off = pos;
-  s.has_t0 = (p.t0_rel_in || p.t0_rel_out) && pos + (size_t)2 * n * sizeof(int32_t) <= DMG_FFT_T0_SMEM_LIMIT;
-  if (s.has_t0) pos += (size_t)2 * n * sizeof(int32_t);
+  s.has_t0_in = p.t0_rel_in && pos + (size_t)n * sizeof(int32_t) <= DMG_FFT_T0_SMEM_LIMIT;
+  if (s.has_t0_in) pos += (size_t)n * sizeof(int32_t);
+  s.has_t0_out = p.t0_rel_out && pos + (size_t)n * sizeof(int32_t) <= DMG_FFT_T0_SMEM_LIMIT;
+  if (s.has_t0_out) pos += (size_t)n * sizeof(int32_t);
   s.total = (pos + 15) & ~(size_t)15;
   return s;
 }
@@ -1381,8 +1384,8 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
     kc.contrib_off = (unsigned)S.contrib_off;
     kc.spos_off = (unsigned)S.spos_off;
     kc.t0_off = (unsigned)S.t0_off;
-    kc.t0_in = S.has_t0 && p.t0_rel_in;
-    kc.t0_out = S.has_t0 && p.t0_rel_out;
+    kc.t0_in = S.has_t0_in;
+    kc.t0_out = S.has_t0_out;
     kc.t0base_in = kc.t0_in ? __ldg(p.in.tab[p.kdim[0]]) : 0;
     kc.t0base_out = kc.t0_out ? __ldg(p.out.tab[p.kdim[0]]) : 0;
     // the transform axis's dimension and step (separable sides)
@@ -1438,8 +1441,9 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
       const int d0 = p.kdim[0], m0 = kc.mult0;
       if (kc.t0_in)
         for (int i = tid; i < n; i += NT) t0[i] = (int32_t)(__ldg(p.in.tab[d0] + i * m0) - kc.t0base_in);
+      int32_t *t0o = t0 + (kc.t0_in ? n : 0);
       if (kc.t0_out)
-        for (int i = tid; i < n; i += NT) t0[n + i] = (int32_t)(__ldg(p.out.tab[d0] + i * m0) - kc.t0base_out);
+        for (int i = tid; i < n; i += NT) t0o[i] = (int32_t)(__ldg(p.out.tab[d0] + i * m0) - kc.t0base_out);
     }
     if (blockIdx.x < ntiles_all) {
       const TileState &st = kc.ts[0];
@@ -1596,7 +1600,8 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
                                     }
                                     store_elem<T>(dst, ad, x, out64, sexp);
                                   },
-                                  kc.t0_out ? reinterpret_cast<const int32_t *>(sm + kc.t0_off) + n : nullptr,
+                                  kc.t0_out ? reinterpret_cast<const int32_t *>(sm + kc.t0_off) + (kc.t0_in ? n : 0)
+                                            : nullptr,
                                   kc.t0base_out);
       TileWalk w(tid, p.store_pos, n, lim1, lim2);
       for (int e0 = 0; !done && e0 < total; e0 += NT * EPT) {
