@@ -694,6 +694,11 @@ __device__ __forceinline__ C2<T> &at_xor(C2<T> *buf, int gxb, int cb) {
   return *reinterpret_cast<C2<T> *>(reinterpret_cast<unsigned char *>(buf) + (gxb ^ cb));
 }
 
+// Lengths whose twiddle tables would take 16 KB or more of a block's shared
+// memory (and with it the second block per SM) read the twiddles through L1
+// from the pass's root table instead.
+__host__ __device__ constexpr bool global_twiddles(int n, size_t es) { return (size_t)n * es >= 16384; }
+
 // Twiddles of the power-of-two stages, staged in shared memory once per
 // block: stage (LP, R) keeps w_{LP R}^{j q} (conjugated for the inverse) at
 // LP - 1 + (q - 1) LP + j, so that a thread's R - 1 twiddles sit at
@@ -746,7 +751,12 @@ __device__ __forceinline__ void stage_pow2(const C2<T> *in, C2<T> *out, const C2
 #pragma unroll
       for (int q = 0; q < R; ++q) {
         C2<T> v = at_xor<T>(in, gxb, Gin::g(q * M) * ES);
-        if (q > 0) v = mul<T>(v, tw[(q - 1) * LP + j]);
+        if constexpr (global_twiddles(NF, sizeof(C2<T>))) {
+          // tws: the pass's root table exp(-2 pi i k / NF)
+          if (q > 0) v = mul<T>(v, root_at<T, SIGN>(tws, j * q * (NF / (LP * R))));
+        } else {
+          if (q > 0) v = mul<T>(v, tw[(q - 1) * LP + j]);
+        }
         a[q] = v;
       }
     } else {
@@ -929,7 +939,7 @@ __host__ __device__ inline SmemLayout smem_layout(const dmg_fft_pass &p, bool fi
   s.buf_b = 2 * one;
   size_t pos = (3 * one + 15) & ~(size_t)15;
   s.roots_off = pos;
-  if (fixed && (DMG_FFT_SMEM_ROOTS || pow2_length(n))) pos += (size_t)n * es;
+  if (fixed && (pow2_length(n) ? !global_twiddles(n, es) : DMG_FFT_SMEM_ROOTS)) pos += (size_t)n * es;
   s.contrib_off = pos;
   pos += (size_t)3 * parts_len(p) * sizeof(int64_t);
   s.spos_off = pos;
@@ -1420,7 +1430,8 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
   {
     const int n = FIXED ? NF : p.n;
     if constexpr (POW2) {
-      pow2_twiddles<T, SIGN, NF>(reinterpret_cast<const C2<T> *>(p.roots), reinterpret_cast<C2<T> *>(sm + 3 * PSTRIDE),
+      if (!global_twiddles(NF, sizeof(C2<T>)))
+        pow2_twiddles<T, SIGN, NF>(reinterpret_cast<const C2<T> *>(p.roots), reinterpret_cast<C2<T> *>(sm + 3 * PSTRIDE),
                                  tid);
     } else if constexpr (FIXED && DMG_FFT_SMEM_ROOTS) {
       C2<T> *sr = reinterpret_cast<C2<T> *>(sm + kc.roots_off);
@@ -1546,7 +1557,8 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
       C2<T> *bufA = reinterpret_cast<C2<T> *>(sm + (POW2 ? PSTRIDE : kc.buf_a));
       C2<T> *bufB = reinterpret_cast<C2<T> *>(sm + (POW2 ? 2 * PSTRIDE : kc.buf_b));
       if constexpr (FIXED) {
-        const C2<T> *rts = POW2 ? reinterpret_cast<const C2<T> *>(sm + 3 * PSTRIDE)
+        const C2<T> *rts = POW2 ? (global_twiddles(NF, sizeof(C2<T>)) ? reinterpret_cast<const C2<T> *>(p.roots)
+                                                                      : reinterpret_cast<const C2<T> *>(sm + 3 * PSTRIDE))
                            : DMG_FFT_SMEM_ROOTS ? reinterpret_cast<const C2<T> *>(sm + kc.roots_off)
                                                 : reinterpret_cast<const C2<T> *>(p.roots);
         res = stages_fixed<T, SIGN, NF, fixed_radix(NF, 1)>(bufA, bufB, bufA, rts,

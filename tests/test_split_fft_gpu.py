@@ -130,7 +130,10 @@ def test_forward_and_inverse_fp32(P, spec, shape, schedule, cuda):
     (16, "packed:block(16,4)|block(32,4)|local(256)", (16, 32, 256)),
     (4, "packed:block(8,2)|frev(4,2,block(8,2))|local(512)", (8, 8, 512)),
     (16, "packed:frev(16,16,block(256,4))|block(8,4)|local(64)", (256, 8, 64)),
-], ids=["16x32x256", "8x8x512", "256x8x64"])
+    # 1024- and 2048-point lines (twiddles read through L1 for the 16-byte types)
+    (4, "packed:block(8,2)|block(4,2)|local(1024)", (8, 4, 1024)),
+    (4, "packed:block(4,2)|block(4,2)|local(2048)", (4, 4, 2048)),
+], ids=["16x32x256", "8x8x512", "256x8x64", "8x4x1024", "4x4x2048"])
 def test_long_lines(P, spec, shape, dtype, cuda):
     r = Run(P, spec, shape, cuda, dtype=dtype, schedule=api.SCHEDULE_LINES)
     tol = TOL_C128 if dtype == api.C128 else TOL_C64
