@@ -80,6 +80,11 @@ struct dmg_fft_pass {
    * 2^31 of the first: the kernel may keep them in shared memory as int32
    * offsets from that entry */
   int32_t t0_rel_in, t0_rel_out;
+  /* a side whose layout is separable over dimensions but two of whose tile
+   * axes (semi_a < semi_b) lie in one dimension: its address is the tables
+   * of the other dimensions plus that dimension's table at the coordinate
+   * both axes make up */
+  int32_t semi_in, semi_out, semi_a, semi_b;
   struct dmg_fft_layout in, out;
 };
 

@@ -340,6 +340,20 @@ static int pass_geometry(const struct dmg_split_impl *im, struct dmg_fft_pass *p
                  (p->kdim[2] < 0 || p->kdim[2] != p->kdim[1]);
   p->sep_in = distinct && !li->ranked;
   p->sep_out = distinct && !lo->ranked;
+  /* exactly two tile axes in one dimension (the third, if any, elsewhere) */
+  p->semi_a = p->semi_b = -1;
+  for (int a = 0; a < 3 && p->semi_a < 0; ++a)
+    for (int b = a + 1; b < 3; ++b)
+      if (p->kdim[a] >= 0 && p->kdim[a] == p->kdim[b]) {
+        const int c = 3 - a - b;
+        if (p->kdim[c] < 0 || p->kdim[c] != p->kdim[a]) {
+          p->semi_a = a;
+          p->semi_b = b;
+        }
+        break;
+      }
+  p->semi_in = !distinct && p->semi_a >= 0 && !li->ranked;
+  p->semi_out = !distinct && p->semi_a >= 0 && !lo->ranked;
   return DMG_OK;
 }
 
@@ -551,6 +565,10 @@ static int impl_upload(struct dmg_split_impl *im) {
 }
 
 /* Forward and inverse pass lists of the split schedule. */
+/* how a pass side is addressed: separable over the tile axes, two axes in
+ * one dimension, or per value */
+static const char *side_kind(int sep, int semi) { return sep ? "" : (semi ? "(shared dim)" : "(per value)"); }
+
 /* A pass's tile axes fastest first in memory, as letters: t the transform
  * axis, a and b the first and second vector axes. */
 static void axis_letters(const int32_t *order, char *out) {
@@ -629,8 +647,8 @@ static int build_passes_split(struct dmg_split_impl *im) {
     axis_letters(p->store_order, so);
     pos += snprintf(im->desc + pos, sizeof(im->desc) - pos,
                     " [t=%d n=%d v1=%d x%d v2=%d x%d tiles=%lld%s in=%s%s out=%s%s]", p->t, p->n, p->v1, p->M1, p->v2,
-                    p->M2, (long long)p->ntiles, p->twiddle ? " tw" : "", lo, p->sep_in ? "" : "(ranked)", so,
-                    p->sep_out ? "" : "(ranked)");
+                    p->M2, (long long)p->ntiles, p->twiddle ? " tw" : "", lo, side_kind(p->sep_in, p->semi_in), so,
+                    side_kind(p->sep_out, p->semi_out));
   }
   return DMG_OK;
 }
@@ -709,7 +727,8 @@ static int build_passes_line(struct dmg_split_impl *im) {
     pos += snprintf(im->desc + pos, sizeof(im->desc) - pos,
                     " [d=%d n=%d v1=%d x%d v2=%d x%d tiles=%lld%s in=%s%s out=%s%s]", p->t / 2, p->n,
                     p->v1 >= 0 ? p->v1 / 2 : -1, p->M1, p->v2 >= 0 ? p->v2 / 2 : -1, p->M2, (long long)p->ntiles,
-                    p->perm_out ? " slots" : "", lo, p->sep_in ? "" : "(ranked)", so, p->sep_out ? "" : "(ranked)");
+                    p->perm_out ? " slots" : "", lo, side_kind(p->sep_in, p->semi_in), so,
+                    side_kind(p->sep_out, p->semi_out));
   }
   return DMG_OK;
 }

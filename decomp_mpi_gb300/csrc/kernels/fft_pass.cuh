@@ -990,7 +990,8 @@ __device__ __forceinline__ void copy_async_wait_all() { asm volatile("cp.async.w
 // covers it (else 0).  The side's address is then L.base + the last three +
 // the tables of the tile axes.
 __device__ __forceinline__ void sep_parts_async(const dmg_fft_layout &L, const dmg_fft_pass &p, const int *yb,
-                                                const int *zb, int lim1, int lim2, int tid, int64_t *part) {
+                                                const int *zb, int lim1, int lim2, int tid, int64_t *part,
+                                                bool semi = false) {
   const int M1 = p.M1;
   const int E = 1 + M1 + p.M2;
   for (int i = tid; i < E + 3; i += NT) {
@@ -1006,7 +1007,9 @@ __device__ __forceinline__ void sep_parts_async(const dmg_fft_layout &L, const d
       const int k = i <= M1 ? 1 : 2;
       const int c = k == 1 ? i - 1 : i - 1 - M1;
       const int d = p.kdim[k];
-      if (d >= 0 && c < (k == 1 ? lim1 : lim2)) {
+      // (a side with two axes in one dimension reads that dimension per value)
+      const bool paired = semi && (k == p.semi_a || k == p.semi_b);
+      if (d >= 0 && !paired && c < (k == 1 ? lim1 : lim2)) {
         const int x = yb[d] + p.A[d] * zb[d] + (p.kisz[k] ? p.A[d] * c : c);
         copy_async<8>(part + i, L.tab[d] + x);
       } else {
@@ -1015,6 +1018,32 @@ __device__ __forceinline__ void sep_parts_async(const dmg_fft_layout &L, const d
     }
   }
 }
+// A side with two tile axes in one dimension: that dimension's table and the
+// coordinate's start and steps along the two axes (x = x0 + sa ca + sb cb),
+// for a tile.
+struct SharedDim {
+  const int64_t *tab;
+  int x0, sa, sb;
+  bool t_paired;  // the transform axis is one of the two
+};
+__device__ __forceinline__ SharedDim shared_dim(const dmg_fft_layout &L, const dmg_fft_pass &p, const int *yb,
+                                                const int *zb) {
+  const int d = p.kdim[p.semi_a];
+  SharedDim s;
+  s.tab = L.tab[d];
+  s.x0 = yb[d] + p.A[d] * zb[d];
+  s.sa = p.kisz[p.semi_a] ? p.A[d] : 1;
+  s.sb = p.kisz[p.semi_b] ? p.A[d] : 1;
+  s.t_paired = p.semi_a == 0;
+  return s;
+}
+// the shared dimension's table entry at tile offsets (c0, c1, c2)
+__device__ __forceinline__ int64_t shared_dim_part(const SharedDim &s, const dmg_fft_pass &p, int c0, int c1, int c2) {
+  const int ca = p.semi_a == 0 ? c0 : c1;  // semi_a < semi_b
+  const int cb = p.semi_b == 1 ? c1 : c2;
+  return __ldg(s.tab + s.x0 + s.sa * ca + s.sb * cb);
+}
+
 // the base of a separable side's addresses in a tile (parts complete)
 __device__ __forceinline__ int64_t sep_base(const dmg_fft_layout &L, const dmg_fft_pass &p, const int64_t *part) {
   const int E = 1 + p.M1 + p.M2;
@@ -1343,7 +1372,7 @@ __device__ __forceinline__ void gather_async(const dmg_fft_pass &p, const PassCo
   const int d0 = kc.d0, mult0 = kc.mult0;
   const int16_t *spos = reinterpret_cast<const int16_t *>(sm + kc.spos_off);
   const int64_t *tab0 = p.in.tab[d0] + (yb[d0] + p.A[d0] * zb[d0]);
-  const int64_t in0 = p.sep_in ? sep_base(p.in, p, pin) : 0;
+  const int64_t in0 = (p.sep_in || p.semi_in) ? sep_base(p.in, p, pin) : 0;
   const unsigned sbase = (unsigned)__cvta_generic_to_shared(sm);  // the staging buffer
   const unsigned char *gsrc = static_cast<const unsigned char *>(bt.src[st.job]);
   if (p.sep_in &&
@@ -1356,12 +1385,17 @@ __device__ __forceinline__ void gather_async(const dmg_fft_pass &p, const PassCo
     copy_async_commit();
     return;
   }
+  const SharedDim sd = p.semi_in ? shared_dim(p.in, p, yb, zb) : SharedDim{};
   TileWalk w(tid, p.load_pos, n, lim1, lim2);
   for (int e = tid; e < total; e += NT, w.next()) {
     const int c0 = w.coord(p.load_pos[0]), c1 = w.coord(p.load_pos[1]), c2 = w.coord(p.load_pos[2]);
     int64_t ad;
     if (p.sep_in) {
       ad = in0 + __ldg(tab0 + c0 * mult0) + pin[1 + c1] + pin[1 + M1 + c2];
+    } else if (p.semi_in) {
+      // the paired axes' parts are zero in pin
+      ad = in0 + shared_dim_part(sd, p, c0, c1, c2) + (sd.t_paired ? 0 : __ldg(tab0 + c0 * mult0)) + pin[1 + c1] +
+           pin[1 + M1 + c2];
     } else {
       int x[DMG_FFT_MAXDIM];
       element_x(p, yb, zb, c0, c1, c2, x);
@@ -1458,8 +1492,9 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
     }
     if (blockIdx.x < ntiles_all) {
       const TileState &st = kc.ts[0];
-      if (p.sep_in) sep_parts_async(p.in, p, st.yb, st.zb, st.lim1, st.lim2, tid, parts_in);
-      if (p.sep_out) sep_parts_async(p.out, p, st.yb, st.zb, st.lim1, st.lim2, tid, parts_out0);
+      if (p.sep_in || p.semi_in) sep_parts_async(p.in, p, st.yb, st.zb, st.lim1, st.lim2, tid, parts_in, p.semi_in);
+      if (p.sep_out || p.semi_out)
+        sep_parts_async(p.out, p, st.yb, st.zb, st.lim1, st.lim2, tid, parts_out0, p.semi_out);
       copy_async_commit();
     }
   }
@@ -1483,9 +1518,11 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
     // scatter side into the area this tile's scatter does not read
     if (next < ntiles_all) {
       const TileState &sn = kc.ts[nxt];
-      if (p.sep_in) sep_parts_async(p.in, p, sn.yb, sn.zb, sn.lim1, sn.lim2, tid, parts_in);
-      if (p.sep_out)
-        sep_parts_async(p.out, p, sn.yb, sn.zb, sn.lim1, sn.lim2, tid, parts_out0 + ((it + 1) & 1) * parts_len(p));
+      if (p.sep_in || p.semi_in)
+        sep_parts_async(p.in, p, sn.yb, sn.zb, sn.lim1, sn.lim2, tid, parts_in, p.semi_in);
+      if (p.sep_out || p.semi_out)
+        sep_parts_async(p.out, p, sn.yb, sn.zb, sn.lim1, sn.lim2, tid, parts_out0 + ((it + 1) & 1) * parts_len(p),
+                        p.semi_out);
       copy_async_commit();
     }
     // convert a complex128 input to double-float, apply the inverse split
@@ -1595,7 +1632,7 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
       const int64_t *pout = parts_out0 + (it & 1) * parts_len(p);
       const int16_t *spos = reinterpret_cast<const int16_t *>(sm + kc.spos_off) + n;
       const int64_t *tab0 = p.out.tab[d0] + (yb[d0] + p.A[d0] * zb[d0]);
-      const int64_t out0 = p.sep_out ? sep_base(p.out, p, pout) : 0;
+      const int64_t out0 = (p.sep_out || p.semi_out) ? sep_base(p.out, p, pout) : 0;
       const bool out64 = kc.out64;
       const int sexp = st.sexp;
       void *dst = bt.dst[st.job];
@@ -1615,6 +1652,7 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
                                   kc.t0_out ? reinterpret_cast<const int32_t *>(sm + kc.t0_off) + (kc.t0_in ? n : 0)
                                             : nullptr,
                                   kc.t0base_out);
+      const SharedDim sdo = p.semi_out ? shared_dim(p.out, p, yb, zb) : SharedDim{};
       TileWalk w(tid, p.store_pos, n, lim1, lim2);
       for (int e0 = 0; !done && e0 < total; e0 += NT * EPT) {
         int64_t ad[EPT];
@@ -1633,6 +1671,9 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
             v[u] = x;
             if (p.sep_out) {
               ad[u] = out0 + __ldg(tab0 + c0 * mult0) + pout[1 + c1] + pout[1 + M1 + c2];
+            } else if (p.semi_out) {
+              ad[u] = out0 + shared_dim_part(sdo, p, c0, c1, c2) + (sdo.t_paired ? 0 : __ldg(tab0 + c0 * mult0)) +
+                      pout[1 + c1] + pout[1 + M1 + c2];
             } else {
               int xg[DMG_FFT_MAXDIM];
               element_x(p, yb, zb, c0, c1, c2, xg);
