@@ -90,6 +90,8 @@ CASES = [
     (4, "packed:block(30,4)", (30,), 0, None),                                 # 1D
     (4, "packed:block(12,2)|block(18,2)", (12, 18), 0, None),                  # 2D
     (64, "packed:frev(16,8,block(128,8))|rotate(3,block(64,8))|local(32)", (128, 64, 32), 0, None),
+    (4, "packed:block(5,4)|local(6)|local(4)", (5, 6, 4), 0, None),          # rank 3 holds nothing
+    (4, "packed:block(6,4)|block(9,1)|local(8)", (6, 9, 8), 0, None),        # uneven blocks 2, 2, 2, 0
 ]
 
 
