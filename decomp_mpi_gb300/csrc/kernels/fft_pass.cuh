@@ -1068,13 +1068,14 @@ struct TileState {
   int job, sexp;
 };
 
-// Values every phase needs.  They live in shared memory and each phase
-// reads them after a barrier, so that none of them holds a register through
-// the FFT stages.
 // The tile index as digits (v1 tile, v2 tile, the batch sub-axes, the job;
 // radices nt1, nt2, blen[], count): a block steps through its tiles by
 // adding the digits of the grid size, without dividing.
 constexpr int NDIG = 9;
+
+// Values every phase needs.  They live in shared memory and each phase
+// reads them after a barrier, so that none of them holds a register through
+// the FFT stages.
 struct PassConsts {
   int ld, M1, d0, mult0, td, v1_ytd, v2_ytd, in64, out64;
   unsigned buf_a, buf_b, roots_off, contrib_off, spos_off, t0_off;
