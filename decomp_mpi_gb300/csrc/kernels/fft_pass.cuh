@@ -694,10 +694,13 @@ __device__ __forceinline__ C2<T> &at_xor(C2<T> *buf, int gxb, int cb) {
   return *reinterpret_cast<C2<T> *>(reinterpret_cast<unsigned char *>(buf) + (gxb ^ cb));
 }
 
-// Lengths whose twiddle tables would take 16 KB or more of a block's shared
-// memory (and with it the second block per SM) read the twiddles through L1
-// from the pass's root table instead.
-__host__ __device__ constexpr bool global_twiddles(int n, size_t es) { return (size_t)n * es >= 16384; }
+// Lengths whose twiddle tables would crowd a block's shared memory (16 KB
+// and more, which costs the second block per SM; for 8-byte values 8 KB,
+// which leaves the room the transform-axis offsets need) read the twiddles
+// through L1 from the pass's root table instead.
+__host__ __device__ constexpr bool global_twiddles(int n, size_t es) {
+  return (size_t)n * es >= (es == 8 ? 8192u : 16384u);
+}
 
 // Twiddles of the power-of-two stages, staged in shared memory once per
 // block: stage (LP, R) keeps w_{LP R}^{j q} (conjugated for the inverse) at
