@@ -797,8 +797,8 @@ def run_precision(args):
 
 def run_fft(args):
     """Split FFT alone: forward and inverse timings (CUDA events, median of 5 after 2 warm-up runs) and per-pass
-    times at n^3 on an 8x8 grid in the factor_reverse decomposition of the headline chain, for the chosen
-    element type and every arithmetic and schedule that applies.  One JSON line."""
+    times at n^3 on a g x g grid (--grid, 8 by default) in the factor_reverse decomposition of the headline chain,
+    for the chosen element type and every arithmetic and schedule that applies.  One JSON line."""
     import torch
 
     from decomp_mpi_gb300 import api
@@ -808,7 +808,9 @@ def run_fft(args):
     dev = torch.device("cuda:0")
     stream = torch.cuda.current_stream(dev)
     sh = stream.cuda_stream
-    _, _, frv = specs(n)
+    gs = args.grid
+    P = gs * gs
+    _, _, frv = specs(n, (gs, gs))
     comm = api.Comm(P)
     D = api.decomp_from_spec(comm, frv)
     tdt = torch.complex128 if dt == api.C128 else torch.complex64
@@ -884,7 +886,7 @@ def run_fft(args):
                     out[key]["graph_forward_inverse_ms"] = None
                     out[key]["graph_error"] = str(err).splitlines()[0][:200]
                 out[key]["eager_forward_inverse_ms"] = round(statistics.median(f) + statistics.median(b), 4)
-    print(json.dumps({"mode": "fft", "n": n, "dtype": args.dtype, "grid": "8x8 virtual",
+    print(json.dumps({"mode": "fft", "n": n, "dtype": args.dtype, "grid": "%dx%d virtual" % (gs, gs),
                       "decomposition": frv, **out}))
 
 
@@ -899,6 +901,7 @@ def main():
     ap.add_argument("--n", type=int, default=N_SIDE, help="cube side (the headline workload is 512)")
     ap.add_argument("--fft", action="store_true", help="split FFT alone at --n: per-arithmetic, per-schedule times")
     ap.add_argument("--dtype", default="c128", choices=["c128", "c64"], help="with --fft: element type")
+    ap.add_argument("--grid", type=int, default=GRID[0], help="with --fft: virtual grid side (g x g ranks)")
     ap.add_argument("--schedule", default="both", choices=["lines", "split", "both"], help="with --fft")
     ap.add_argument("--serve", action="store_true", help="served form: Poisson stream of mixed-size jobs")
     ap.add_argument("--precision", action="store_true", help="precision form: 1024^3 complex64 with error")
