@@ -161,6 +161,29 @@ def test_delta_input_known_answer(cuda):
     assert np.array_equal(got[mask], np.ones(mask.sum(), np.complex128))
 
 
+@pytest.mark.parametrize("schedule", [api.SCHEDULE_LINES, api.SCHEDULE_SPLIT], ids=["lines", "split"])
+def test_point_input_phase_ramp(schedule, cuda):
+    """fftw_test.c:93-98's POINT input, a delta at (0, 0, 1): the forward transform is the analytic phase ramp
+    exp(-2 pi i k2 / L2), placed in the B layout's slots (slot s holds frequency s / A + B * (s % A))."""
+    import torch
+    P, spec, shape = 4, "packed:block(16,2)|block(12,2)|local(20)", (16, 12, 20)
+    r = Run(P, spec, shape, cuda, schedule=schedule)
+    off = O.global_offsets(P, spec, r.dp, shape)
+    host = np.zeros(P * r.dp, np.complex128)
+    host[off[0, 0, 1]] = 1.0
+    r.dat.copy_(torch.from_numpy(host))
+    got = r.forward()
+    A, B, _, _, a_spec, b_spec = O.split_factors(P, spec)
+    out_spec = a_spec if all(a == 1 for a in A) else b_spec
+    s2 = np.arange(shape[2])
+    k2 = s2 // A[2] + B[2] * (s2 % A[2])
+    ramp = np.broadcast_to(np.exp(-2j * np.pi * k2 / shape[2]), shape)
+    want = np.zeros(P * r.wl, np.complex128)
+    want[O.global_offsets(P, out_spec, r.wl, shape).ravel()] = ramp.ravel()
+    _, mask = O.split_expected_output(P, spec, np.zeros(shape), r.wl)
+    assert np.max(np.abs(got[mask] - want[mask])) < 1e-13
+
+
 def test_linear_index_pattern_roundtrip(cuda):
     """split_plan_test.c's pattern value = i + L*(j + L*k), forward then backward, scaled by 1/N^3."""
     import torch
