@@ -20,7 +20,7 @@ transforms at 5 N log2 N flops each, divided by the time of the full step,
 reshapes included); the reshape GB/s and the FFT-only GFLOP/s are reported
 beside it.  ``--impl reference`` times the reference algorithm on the host
 cores instead (the CPU restatement under oracle/: the reference itself needs
-MPI and FFTW, which the GPU machine does not have).
+MPI and FFTW, which the GB300 host does not have).
 """
 from __future__ import annotations
 
@@ -270,7 +270,7 @@ def run_gpu(args):
     sp.run(api.FFTW_FORWARD, sh)
     sp.run(api.FFTW_BACKWARD, sh)
     torch.cuda.synchronize()
-    from oracle import oracle as O  # the checker only
+    from oracle import oracle as O  # the parity check only
     off = torch.from_numpy(O.global_offsets(P, frv, r12.dest_pitch, (n,) * 3).ravel()).to(dev)
     back = a2[off] / n_total
     want = ref[off]
@@ -663,7 +663,7 @@ def run_serve(args):
         comm = api.Comm(P)
         pb = api.decomp_from_spec(comm, blk).extent()
         pr = api.decomp_from_spec(comm, rot).extent()
-        from oracle import oracle as O  # the checker only
+        from oracle import oracle as O  # the parity check only
         hi, hs, ho = bufs[(side, dt)]
         gin = O.gather_global(P, blk, hi.numpy().astype(np.complex128), pb, (side,) * 3)
         gout = O.gather_global(P, rot, ho.numpy().astype(np.complex128), pr, (side,) * 3) / side ** 3

@@ -1,6 +1,6 @@
 /*
  * TEST INFRASTRUCTURE (oracle).  CPU restatement of the reference's reshape
- * and split-FFT algorithms, used only as the checker in tests, by the smoke
+ * and split-FFT algorithms, used only to check results in tests, by the smoke
  * check, and as the benchmark's CPU baseline.  Never linked into the product.
  *
  * Decompositions are given as spec strings (spec.h) over P virtual ranks;
