@@ -1,6 +1,6 @@
 // Device throughput probe: the FP64 and FP32 FMA rates of the GPU the
 // library runs on, used as the roofline denominator of the FP64 FFT passes
-// (the measured peaks cover HBM and bf16 tensor throughput only).
+// (the measured peaks file covers HBM and bf16 tensor throughput only).
 #include <cuda_runtime.h>
 #include "../host/dmg_internal.h"
 
