@@ -417,7 +417,7 @@ DmgServer dmg_server_create(int grid, long long arena_bytes, int slots, int max_
   void *base = NULL;
   if (dmg_dev_alloc(&base, (size_t)arena_bytes) != DMG_OK) goto fail;
   s->base = (char *)base;
-  s->ar.size = arena_bytes;
+  s->ar.size = arena_bytes / ALIGN * ALIGN; /* what the free list can hand out: a job larger never fits */
   s->ar.cap = 16;
   s->ar.free = (blk *)calloc(16, sizeof(blk));
   if (!s->ar.free) goto fail;
@@ -485,7 +485,7 @@ long long dmg_server_submit(DmgServer s, const dmg_job *job) {
 }
 
 int dmg_server_poll(DmgServer s, dmg_job_done *done, int max) {
-  if (!s || (!done && max > 0)) return -dmg_error(DMG_ERR_ARG, "dmg_server_poll: bad arguments");
+  if (!s || max < 0 || (!done && max > 0)) return -dmg_error(DMG_ERR_ARG, "dmg_server_poll: bad arguments");
   pthread_mutex_lock(&s->mu);
   int n = s->ndone < max ? s->ndone : max;
   for (int i = 0; i < n; ++i) {
