@@ -172,6 +172,41 @@ def test_sweep_256_cubed(kind, tdt, cuda):
     _index_roundtrip(g * g, blk, other, (n, n, n), getattr(torch, tdt), cuda)
 
 
+LARGEST = [
+    ((1024, 1024, 512), 32, "packed:frev(16,64,block(1024,32))|frev(64,16,block(1024,32))|local(512)"),
+    ((512, 512, 1024), 16, "packed:interleave(block(32,16),16)|interleave(block(32,16),16)|local(1024)"),
+]
+
+
+@pytest.mark.parametrize("shape,g,other", LARGEST, ids=["1024x1024x512-32x32-frev", "512x512x1024-16x16-interleave"])
+def test_sweep_largest_arrays(shape, g, other, cuda):
+    """The reshape sweep's largest arrays, 4 GiB over 1024 virtual ranks and 2 GiB over 256, in 8-byte
+    elements (int64 or complex64: the move is the same).  The source holds every slot's global linear
+    index; the reshape must give that pattern in the destination decomposition (both patterns written
+    by the device index visitor, which its own tests pin to the oracle), and the reverse reshape must
+    restore the source exactly."""
+    import torch
+    P = g * g
+    L0, L1, L2 = shape
+    comm = api.Comm(P)
+    S = api.decomp_from_spec(comm, "packed:block(%d,%d)|block(%d,%d)|local(%d)" % (L0, g, L1, g, L2))
+    D = api.decomp_from_spec(comm, other)
+    fwd, bwd = api.ReshapePlan(comm, 8, S, D), api.ReshapePlan(comm, 8, D, S)
+    st = torch.cuda.current_stream(cuda).cuda_stream
+    src = torch.full((P * fwd.src_pitch,), -1, dtype=torch.int64, device=cuda)
+    want = torch.full((P * fwd.dest_pitch,), -7, dtype=torch.int64, device=cuda)
+    api.fill_index(S, 8, src.data_ptr(), st)
+    api.fill_index(D, 8, want.data_ptr(), st)
+    dst = torch.full_like(want, -7)
+    fwd.run(src.data_ptr(), dst.data_ptr(), st)
+    back = torch.full_like(src, -1)
+    bwd.run(dst.data_ptr(), back.data_ptr(), st)
+    torch.cuda.synchronize()
+    assert int((src >= 0).sum()) == L0 * L1 * L2
+    assert torch.equal(dst, want)
+    assert torch.equal(back, src)
+
+
 def test_cuda_graph_replay(cuda):
     """A reshape run captured into a CUDA graph (after a first run has put its tables on the device)
     replays to the eager result; a second source buffer gives its own permutation."""
