@@ -72,7 +72,9 @@ def build(verbose: bool = False, force: bool = False) -> str:
             jobs.append([NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                          "--expt-relaxed-constexpr", *NVCC_EXTRA, *incs, "-c", s, "-o", o])
     if jobs:
-        with ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
+        # the pass kernels take longest: start them first, on every host core
+        jobs.sort(key=lambda j: (j[0] != NVCC, -os.path.getsize(j[-3])))
+        with ThreadPoolExecutor(max_workers=min(max(8, os.cpu_count() or 8), len(jobs))) as ex:
             outs = list(ex.map(_run, jobs))
         if verbose:
             for j, o in zip(jobs, outs):

@@ -1,6 +1,6 @@
-// Batched FFT pass with fused layout change (shared by the per-arithmetic
-// and per-direction translation units fft_pass_{f64,f32,df}.cu and
-// fft_pass_{f64,f32,df}_inv.cu).
+// Batched FFT pass with fused layout change (shared by the translation units
+// fft_pass_{f64,f32,df}{,_inv}{,_mixed}.cu: one per arithmetic, direction and
+// group of lengths).
 //
 // One launch transforms every line along one axis and writes the result in
 // another layout.  A block owns tiles of n x M1 x M2 values, persistent over
@@ -1717,8 +1717,15 @@ int launch_k(const dmg_fft_pass &p, const dmg_fft_batch &bt, cudaStream_t s) {
   return DMG_OK;
 }
 
+// The compile-time lengths fall in two groups, each compiled in its own
+// translation unit per arithmetic and direction so that the build runs them
+// in parallel: the powers of two from 8 to 2048, and the other lengths with
+// the runtime-length kernel.
+__host__ __device__ constexpr bool pow2_group(int n) { return n >= 8 && n <= 2048 && (n & (n - 1)) == 0; }
+
 template <typename T, int SIGN>
-int launch_sign(const dmg_fft_pass &p, const dmg_fft_batch &bt, cudaStream_t s) {
+int launch_pow2_group(const dmg_fft_pass &p, const dmg_fft_batch &bt, void *stream) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
   switch (p.n) {
     case 8: return launch_k<T, SIGN, 8>(p, bt, s);
     case 16: return launch_k<T, SIGN, 16>(p, bt, s);
@@ -1729,6 +1736,14 @@ int launch_sign(const dmg_fft_pass &p, const dmg_fft_batch &bt, cudaStream_t s) 
     case 512: return launch_k<T, SIGN, 512>(p, bt, s);
     case 1024: return launch_k<T, SIGN, 1024>(p, bt, s);
     case 2048: return launch_k<T, SIGN, 2048>(p, bt, s);
+    default: return dmg_error(DMG_ERR_ARG, "fft pass: length %d is not a power of two from 8 to 2048", p.n);
+  }
+}
+
+template <typename T, int SIGN>
+int launch_other_group(const dmg_fft_pass &p, const dmg_fft_batch &bt, void *stream) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  switch (p.n) {
     case 48: return launch_k<T, SIGN, 48>(p, bt, s);
     case 96: return launch_k<T, SIGN, 96>(p, bt, s);
     case 120: return launch_k<T, SIGN, 120>(p, bt, s);
@@ -1742,12 +1757,10 @@ int launch_sign(const dmg_fft_pass &p, const dmg_fft_batch &bt, cudaStream_t s) 
   }
 }
 
-// Launch one pass of direction SIGN (p.sign) over a batch of jobs in
-// arithmetic T (checked by the caller).  The two directions are compiled in
-// separate translation units.
-template <typename T, int SIGN>
-int launch_pass(const dmg_fft_pass &p, const dmg_fft_batch &bt, void *stream) {
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
+// Checks of a pass launch over a batch of jobs in arithmetic T, before the
+// launch in the direction p.sign goes to the translation unit of its group.
+template <typename T>
+int check_batch(const dmg_fft_pass &p, const dmg_fft_batch &bt) {
   if (bt.count < 1 || bt.count > DMG_FFT_MAXBATCH)
     return dmg_error(DMG_ERR_ARG, "fft pass: batch of %d jobs (1 to %d)", bt.count, DMG_FFT_MAXBATCH);
   for (int j = 0; j < bt.count; ++j) {
@@ -1757,7 +1770,7 @@ int launch_pass(const dmg_fft_pass &p, const dmg_fft_batch &bt, void *stream) {
     if (std::is_same<T, df>::value && (p.in_fp64 || p.out_fp64) && !bt.scale_exp[j])
       return dmg_error(DMG_ERR_ARG, "double-float pass without a scale exponent");
   }
-  return launch_sign<T, SIGN>(p, bt, s);
+  return DMG_OK;
 }
 
 template <typename T>

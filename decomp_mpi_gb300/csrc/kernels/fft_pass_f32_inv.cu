@@ -1,6 +1,6 @@
-// FFT pass kernels in one arithmetic (f32), inverse direction; see fft_pass.cuh.
+// FFT pass kernels in one arithmetic (float), inverse direction, power-of-two lengths; see fft_pass.cuh.
 #include "fft_pass.cuh"
 
-int dmg_fft_pass_launch_f32_inv(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream) {
-  return launch_pass<float, 1>(*p, *b, stream);
+int dmg_fft_pass_f32_inv_pow2(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream) {
+  return launch_pow2_group<float, 1>(*p, *b, stream);
 }

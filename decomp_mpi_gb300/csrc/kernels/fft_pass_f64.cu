@@ -1,12 +1,20 @@
-// FFT pass kernels in one arithmetic (double); see fft_pass.cuh.
+// FFT pass kernels in one arithmetic (double): the checks and the choice of
+// translation unit, and the forward direction's power-of-two lengths; see fft_pass.cuh.
 #include "fft_pass.cuh"
 
 size_t dmg_fft_pass_smem_f64(const dmg_fft_pass *p) { return pass_smem<double>(*p); }
 
-// the inverse direction's kernels (fft_pass_f64_inv.cu)
-int dmg_fft_pass_launch_f64_inv(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream);
+// the other groups of lengths and the inverse direction (fft_pass_f64_inv.cu,
+// fft_pass_f64_mixed.cu, fft_pass_f64_inv_mixed.cu)
+int dmg_fft_pass_f64_inv_pow2(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream);
+int dmg_fft_pass_f64_fwd_mixed(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream);
+int dmg_fft_pass_f64_inv_mixed(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream);
 
 int dmg_fft_pass_launch_f64(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream) {
-  if (p->sign > 0) return dmg_fft_pass_launch_f64_inv(p, b, stream);
-  return launch_pass<double, -1>(*p, *b, stream);
+  const int st = check_batch<double>(*p, *b);
+  if (st != DMG_OK) return st;
+  const bool inv = p->sign > 0;
+  if (pow2_group(p->n))
+    return inv ? dmg_fft_pass_f64_inv_pow2(p, b, stream) : launch_pow2_group<double, -1>(*p, *b, stream);
+  return inv ? dmg_fft_pass_f64_inv_mixed(p, b, stream) : dmg_fft_pass_f64_fwd_mixed(p, b, stream);
 }

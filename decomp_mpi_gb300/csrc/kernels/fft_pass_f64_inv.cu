@@ -1,6 +1,6 @@
-// FFT pass kernels in one arithmetic (f64), inverse direction; see fft_pass.cuh.
+// FFT pass kernels in one arithmetic (double), inverse direction, power-of-two lengths; see fft_pass.cuh.
 #include "fft_pass.cuh"
 
-int dmg_fft_pass_launch_f64_inv(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream) {
-  return launch_pass<double, 1>(*p, *b, stream);
+int dmg_fft_pass_f64_inv_pow2(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream) {
+  return launch_pow2_group<double, 1>(*p, *b, stream);
 }
