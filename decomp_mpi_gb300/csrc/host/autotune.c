@@ -9,7 +9,8 @@
  * (the reference's GUESS_GRID variant, split_fft.c:197-201), because on one
  * GPU the grid only relabels which virtual rank holds a block and the full
  * grid search multiplies the candidates by the grid count;
- * full_grid_search = 1 walks every grid as the reference does.
+ * full_grid_search = 1 walks every grid as the reference does.  Each
+ * candidate is timed in both pass schedules where its lengths allow both.
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -37,17 +38,33 @@ typedef struct {
   int tried;
 } tune_ctx;
 
-static void time_candidate(tune_ctx *c, SplitPlan cand) {
-  if (!cand) return;
+/* One untimed run uploads the tables, then one timed run (SEARCH_TRIAL =
+ * SEARCH_REPEAT = 1 in the reference). */
+static int time_forward(tune_ctx *c, SplitPlan cand, float *ms) {
   void *s = dmg_current_stream();
-  float ms = 0;
-  /* one untimed run uploads the tables, then one timed run (SEARCH_TRIAL =
-   * SEARCH_REPEAT = 1 in the reference) */
   if (dmg_split_run(cand, FFTW_FORWARD, s) != DMG_OK || dmg_split_record_event(c->ev, 0, s) != DMG_OK ||
       dmg_split_run(cand, FFTW_FORWARD, s) != DMG_OK || dmg_split_record_event(c->ev, 1, s) != DMG_OK ||
-      dmg_split_event_elapsed(c->ev, 0, 1, &ms) != DMG_OK) {
+      dmg_split_event_elapsed(c->ev, 0, 1, ms) != DMG_OK)
+    return DMG_ERR_CUDA;
+  return DMG_OK;
+}
+
+/* Times a candidate in its default pass schedule and, where the plan allows
+ * it, in the other one (one pass per dimension, or the reference's two
+ * stages), and keeps the faster schedule on the plan. */
+static void time_candidate(tune_ctx *c, SplitPlan cand) {
+  if (!cand) return;
+  float ms = 0;
+  if (time_forward(c, cand, &ms) != DMG_OK) {
     freeSplitPlan(cand);
     return;
+  }
+  const int first = dmg_split_get_schedule(cand);
+  const int other = first == DMG_SCHEDULE_LINES ? DMG_SCHEDULE_SPLIT : DMG_SCHEDULE_LINES;
+  if (dmg_split_set_schedule(cand, other) == DMG_OK) {
+    float ms2 = 0;
+    if (time_forward(c, cand, &ms2) == DMG_OK && ms2 > 0 && ms2 < ms) ms = ms2;
+    else dmg_split_set_schedule(cand, first);
   }
   c->tried++;
   if (ms > 0 && ms < c->best_ms) {
