@@ -17,6 +17,7 @@ from ._lib import DecompError, check, last_error, load
 
 __all__ = [
     "Comm", "Decomp", "ReshapePlan", "SplitPlan", "decomp_from_spec", "processor_grid", "DecompError",
+    "propose_parallel_plan", "build_parallel_plan",
     "FFTW_FORWARD", "FFTW_BACKWARD", "C128", "C64",
 ]
 
@@ -30,6 +31,11 @@ ARITH_DF = 2
 SCHEDULE_AUTO = 0
 SCHEDULE_LINES = 1
 SCHEDULE_SPLIT = 2
+# SearchFlags of split_fft.h
+NO_FLAGS = 0x00
+PREFER_LARGE_FFT = 0x01
+PREFER_STAGE1 = 0x02
+FORCE_USE_FIRST = 0x04
 
 
 class _DecompStruct(ctypes.Structure):
@@ -480,6 +486,39 @@ class SplitPlan:
             self.free()
         except Exception:
             pass
+
+
+def _wrap_plan(start: Decomp, handle, length: int) -> "SplitPlan":
+    sp = SplitPlan.__new__(SplitPlan)
+    sp.lib, sp.start, sp.h, sp.length, sp.dtype = load(), start, handle, int(length), C128
+    return sp
+
+
+def propose_parallel_plan(flags: int, start: Decomp, B, dat_ptr: int, length: int, work_ptr: int):
+    """proposeParallelPlan: the plan of the given second-stage factors B (A = L / B), grids from
+    makeProcessorGrid; None where the reference declines (every B_i = 1 under PREFER_STAGE1)."""
+    lib = load()
+    lib.dmg_clear_error()
+    h = lib.proposeParallelPlan(int(flags), start.h, _int_array(B), ctypes.c_void_p(dat_ptr), int(length),
+                                ctypes.c_void_p(work_ptr))
+    if not h:
+        if lib.dmg_last_error_code():
+            raise DecompError("proposeParallelPlan: %s" % last_error())
+        return None
+    return _wrap_plan(start, h, length)
+
+
+def build_parallel_plan(flags: int, use_first: int, use_second: int, start: Decomp, A, B, L, grid_a, grid_b,
+                        dat_ptr: int, length: int, work_ptr: int):
+    """buildParallelPlan: the plan of explicit factors and processor grids for the A and B stages."""
+    lib = load()
+    nd = len(L)
+    h = lib.buildParallelPlan(int(flags), int(use_first), int(use_second), start.h, nd, _int_array(A), _int_array(B),
+                              _int_array(L), _int_array(grid_a), _int_array(grid_b), ctypes.c_void_p(dat_ptr),
+                              int(length), ctypes.c_void_p(work_ptr))
+    if not h:
+        raise DecompError("buildParallelPlan: %s" % last_error())
+    return _wrap_plan(start, h, length)
 
 
 # ---------------------------------------------------------------- global-order I/O

@@ -112,3 +112,53 @@ def test_gcd():
     lib = api.load()
     for u, v in [(0, 5), (5, 0), (12, 18), (17, 5), (1 << 20, 3 << 10)]:
         assert lib.gcd(u, v) == np.gcd(u, v)
+
+
+def _plan_offsets(dec, shape, wl):
+    import itertools
+    return [dec.global_offset(list(x), wl) for x in itertools.product(*[range(n) for n in shape])]
+
+
+def test_propose_parallel_plan_is_make_parallel_plan():
+    """proposeParallelPlan with no flags (split_fft.c:747-787) is the plan makeParallelPlan builds: the same
+    factors and the same A and B layouts."""
+    P, spec, shape, B = 4, "packed:local(8)|block(12,2)|block(16,2)", (8, 12, 16), [2, 3, 4]
+    c, S = _shape(P, spec)
+    wl = _work_len(shape)
+    sp = api.propose_parallel_plan(api.NO_FLAGS, S, B, 0x100000, wl, 0x200000)
+    ref = api.SplitPlan(S, 0x100000, wl, 0x200000, B=B)
+    assert sp.A_factors == ref.A_factors == [4, 4, 4]
+    assert _plan_offsets(sp.decomp_A(), shape, wl) == _plan_offsets(ref.decomp_A(), shape, wl)
+    assert _plan_offsets(sp.decomp_B(), shape, wl) == _plan_offsets(ref.decomp_B(), shape, wl)
+
+
+def test_propose_parallel_plan_declines_and_rejects():
+    """Every B_i = 1 is declined (NULL, no error) under PREFER_STAGE1 and planned without it; a factor
+    that does not divide its length is an error (the reference aborts, split_fft.c:761-763)."""
+    P, spec, shape = 4, "packed:local(8)|block(12,2)|block(16,2)", (8, 12, 16)
+    c, S = _shape(P, spec)
+    wl = _work_len(shape)
+    assert api.propose_parallel_plan(api.PREFER_STAGE1, S, [1, 1, 1], 0x100000, wl, 0x200000) is None
+    sp = api.propose_parallel_plan(api.NO_FLAGS, S, [1, 1, 1], 0x100000, wl, 0x200000)
+    assert sp.A_factors == [8, 12, 16]
+    with pytest.raises(api.DecompError):
+        api.propose_parallel_plan(api.NO_FLAGS, S, [3, 3, 4], 0x100000, wl, 0x200000)
+
+
+def test_build_parallel_plan_explicit_grids():
+    """buildParallelPlan with explicit processor grids: A's owner depends only on the dimensions its grid
+    splits (grid (1, 2, 2): not on x0), B's likewise (grid (2, 2, 1): not on x2), over all four ranks."""
+    import itertools
+    P, spec, shape = 4, "packed:local(8)|block(12,2)|block(16,2)", (8, 12, 16)
+    c, S = _shape(P, spec)
+    wl = _work_len(shape)
+    sp = api.build_parallel_plan(api.NO_FLAGS, 0, 0, S, [4, 4, 4], [2, 3, 4], list(shape), [1, 2, 2], [2, 2, 1],
+                                 0x100000, wl, 0x200000)
+    assert sp.A_factors == [4, 4, 4]
+    A, B = sp.decomp_A(), sp.decomp_B()
+    own_a, own_b = {}, {}
+    for x in itertools.product(*[range(n) for n in shape]):
+        own_a.setdefault(x[1:], set()).add(A.owner(list(x)))
+        own_b.setdefault(x[:2], set()).add(B.owner(list(x)))
+    assert all(len(v) == 1 for v in own_a.values()) and all(len(v) == 1 for v in own_b.values())
+    assert set().union(*own_a.values()) == set().union(*own_b.values()) == {0, 1, 2, 3}
