@@ -1268,7 +1268,8 @@ void visitData(Decomp d, data_visitor vis, double *dat) {
   int nd = d->ndim;
   int pos[DMG_MAXAX], slot[DMG_MAXAX], gpos[DMG_MAXAX];
   long long total = 1;
-  int view = d->comm->rank;
+  /* the rank the descriptor's fields describe (max_local, isLocal): the view rank when it was made */
+  int view = myRank(d);
   for (int i = 0; i < nd; ++i) total *= (long long)d->dims[i]->max_local + 1;
   for (long long e = 0; e < total; ++e) {
     long long rem = e, off = 0;

@@ -77,8 +77,9 @@ typedef struct split_fft_plan *SplitPlan;
  * (reference split_fft.h:50).  global_position holds the slot's global
  * coordinate, or -1 entries for a slot that holds no data. */
 typedef void (*data_visitor)(int ndim, int *global_position, double *dat);
-/** Visit every slot 0..max_local of the view rank's buffer (host memory,
- * interleaved complex doubles) (reference split_fft.h:51). */
+/** Visit every slot 0..max_local of the buffer of the rank the descriptor
+ * describes (the communicator's view rank when it was made), in host memory
+ * as interleaved complex doubles (reference split_fft.h:51). */
 void visitData(Decomp d, data_visitor vis, double *dat);
 
 /** Build a plan for given factors and grids (reference split_fft.h:52).

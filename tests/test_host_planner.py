@@ -141,3 +141,53 @@ def test_view_rank_fields():
     assert lib.myRank(d.h) == 3
     for pos in [(0, 0), (7, 7), (4, 3)]:
         assert d.owner(pos) == (pos[0] // 4) * 2 + pos[1] // 4
+
+
+VISIT_SPECS = [
+    (4, "axes:rotate(3,block(10,2))@1,1|rotate(3,block(10,2))@5,2"),
+    (4, "packed:local(8)|block(12,2)|block(16,2)"),
+    (6, "packed:block(10,3)|block(7,2)|local(9)"),
+    (4, "packed:interleave(block(4,2),2)|local(12)|interleave(block(4,2),4)"),
+    (5, "packed:block(11,5)|local(6)"),
+]
+
+
+@pytest.mark.parametrize("P,spec", VISIT_SPECS)
+def test_visit_data_slots_and_positions(P, spec):
+    """visitData (reference split_fft.c:862-889) calls the visitor once per slot 0..max_local of the
+    buffer of the rank the descriptor describes; here the position is the slot's global coordinate (-1
+    entries where the slot holds nothing), which must match the oracle's offsets on every rank."""
+    import ctypes
+    c, d = _shape(P, spec)
+    lib = load()
+
+    class AD(ctypes.Structure):
+        _fields_ = [("decomp", ctypes.c_void_p)]
+
+    class DS(ctypes.Structure):
+        _fields_ = [("ndim", ctypes.c_int), ("comm", ctypes.c_void_p), ("proc_used", ctypes.c_int),
+                    ("dims", ctypes.POINTER(ctypes.c_void_p))]
+    ds = DS.from_address(d.h)
+    sizes = tuple(lib.sizeDimDecomp(AD.from_address(ds.dims[i]).decomp) for i in range(ds.ndim))
+    pitch = d.extent()
+    off = O.global_offsets(P, spec, pitch, sizes)
+    VIS = ctypes.CFUNCTYPE(None, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double))
+    lib.visitData.restype, lib.visitData.argtypes = None, [ctypes.c_void_p, VIS, ctypes.POINTER(ctypes.c_double)]
+    for r in range(P):
+        # like an MPI rank, the view rank makes its own descriptor, whose fields describe it
+        c.set_view_rank(r)
+        d = api.decomp_from_spec(c, spec)
+        buf = (ctypes.c_double * (2 * pitch))()
+        seen = {}
+
+        def visit(nd, pos, dat):
+            slot = (ctypes.addressof(dat.contents) - ctypes.addressof(buf)) // 16
+            assert 0 <= slot < pitch
+            seen.setdefault(slot, []).append(tuple(pos[i] for i in range(nd)))
+
+        cb = VIS(visit)
+        lib.visitData(d.h, cb, buf)
+        held = {int(o % pitch): g for g, o in np.ndenumerate(off) if o >= 0 and o // pitch == r}
+        got = {s: p[0] for s, p in seen.items() if -1 not in p[0]}
+        assert got == held
+        assert all(len(p) == 1 for p in seen.values())
