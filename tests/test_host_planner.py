@@ -191,3 +191,24 @@ def test_visit_data_slots_and_positions(P, spec):
         got = {s: p[0] for s, p in seen.items() if -1 not in p[0]}
         assert got == held
         assert all(len(p) == 1 for p in seen.values())
+
+
+@pytest.mark.parametrize("A,B", [(3, 4), (4, 3), (2, 6), (12, 1)])
+def test_factor_reverse_axis_decomp(A, B):
+    """makeFactorReverseAxisDecomp (reference factor_reverse_decomp.c:56-58): the axis of
+    factor_reverse(A, B, nested) keeps the original axis's memory and rank strides."""
+    import ctypes
+    lib = load()
+    P = 4
+    c = api.Comm(P)
+    ax0 = lib.makeAxisDecomp(c.h, lib.makeBlockDecomp(12, 2), 1, 1)
+    fr = lib.makeFactorReverseAxisDecomp(A, B, ax0)
+    ax1 = lib.makeAxisDecomp(c.h, lib.makeBlockDecomp(8, 2), 6, 2)
+    D = api.Decomp(c, lib.makeDecomp(2, (ctypes.c_void_p * 2)(fr, ax1)))
+    lib.freeAxisDecomp(ax0)
+    spec = "axes:frev(%d,%d,block(12,2))@1,1|block(8,2)@6,2" % (A, B)
+    pitch = O.pitch_of(P, spec)
+    assert D.extent() == pitch
+    want = O.global_offsets(P, spec, pitch, (12, 8))
+    for g in np.ndindex(12, 8):
+        assert D.global_offset(list(g), pitch) == want[g]
