@@ -1,0 +1,115 @@
+"""The reference's smaller C entry points through the C-ABI, against the reference's semantics and the
+oracle (no GPU): run-length index sets, the locality and offset queries of a descriptor's view rank,
+the stage decompositions of the split FFT, and DimDecomp cloning."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from decomp_mpi_gb300 import api
+from decomp_mpi_gb300._lib import load
+from oracle import oracle as O
+
+
+class _Index(ctypes.Structure):
+    _fields_ = [("size", ctypes.c_int), ("count", ctypes.c_int), ("offsets", ctypes.POINTER(ctypes.c_int)),
+                ("counts", ctypes.POINTER(ctypes.c_int))]
+
+
+def _runs(h):
+    ix = _Index.from_address(h)
+    return [(ix.offsets[i], ix.counts[i]) for i in range(ix.count)]
+
+
+def test_index_runs():
+    """addIndex merges an offset that continues the last run and starts a new run otherwise; the arrays
+    grow past their initial 16 entries (reference index.c:23-42)."""
+    lib = load()
+    h = lib.makeIndex()
+    for o in [0, 1, 2, 5, 6, 9, 3]:
+        lib.addIndex(h, o)
+    assert _runs(h) == [(0, 3), (5, 2), (9, 1), (3, 1)]
+    assert lib.sizeIndex(h) == 7
+    lib.freeIndex(h)
+    h = lib.makeIndex()
+    for o in range(0, 80, 2):
+        lib.addIndex(h, o)
+    assert _runs(h) == [(o, 1) for o in range(0, 80, 2)]
+    assert _Index.from_address(h).size >= 40
+    lib.freeIndex(h)
+
+
+LOCAL_SPECS = [
+    (4, "packed:local(8)|block(12,2)|rotate(3,block(16,2))", (8, 12, 16)),
+    (6, "packed:block(10,3)|frev(7,1,block(7,2))|local(9)", (10, 7, 9)),
+    (4, "packed:interleave(block(4,2),2)|local(5)|interleave(block(4,2),3)", (8, 5, 12)),
+]
+
+
+@pytest.mark.parametrize("P,spec,shape", LOCAL_SPECS)
+def test_locality_and_offsets_of_the_view_rank(P, spec, shape):
+    """isCoordLocal / areCoordsLocal / getOffset / myRank (reference reshape.h:185-201) describe the rank
+    that made the descriptor: a coordinate is local where the oracle puts it in that rank's buffer, at the
+    oracle's offset inside the buffer."""
+    lib = load()
+    c = api.Comm(P)
+    pitch = O.pitch_of(P, spec)
+    off = O.global_offsets(P, spec, pitch, shape)
+    for r in range(P):
+        c.set_view_rank(r)
+        d = api.decomp_from_spec(c, spec)
+        assert lib.myRank(d.h) == r
+        for g in np.ndindex(*shape):
+            pos = (ctypes.c_int * len(shape))(*g)
+            mine = bool(off[g] >= 0 and off[g] // pitch == r)
+            assert bool(lib.areCoordsLocal(d.h, pos)) == mine
+            if mine:
+                assert lib.getOffset(d.h, pos) == off[g] % pitch
+        # per dimension: a position is local when some held coordinate of the rank has it
+        for dim, n in enumerate(shape):
+            held = {g[dim] for g in np.ndindex(*shape) if off[g] >= 0 and off[g] // pitch == r}
+            for x in range(n):
+                assert bool(lib.isCoordLocal(d.h, dim, x)) == (x in held)
+
+
+def _ints(v):
+    return (ctypes.c_int * len(v))(*v)
+
+
+@pytest.mark.parametrize("A,B,grid", [([4, 3, 2], [2, 4, 5], [2, 2, 1]), ([8, 1, 6], [1, 12, 2], [1, 2, 2])])
+def test_stage_decompositions(A, B, grid):
+    """makeInterleavedDecomp is interleave(block(A_i, grid_i), B_i) per dimension and makeBlockedDecomp is
+    block of A_i B_i with factor A_i over grid_i, both packed (reference split_fft.c:36-77)."""
+    lib = load()
+    P = 4
+    c = api.Comm(P)
+    shape = tuple(a * b for a, b in zip(A, B))
+    for maker, dims in [
+        (lib.makeInterleavedDecomp, ["interleave(block(%d,%d),%d)" % (a, g, b) for a, b, g in zip(A, B, grid)]),
+        (lib.makeBlockedDecomp, ["blockf(%d,%d,%d)" % (a * b, a, g) for a, b, g in zip(A, B, grid)]),
+    ]:
+        d = api.Decomp(c, maker(len(A), c.h, _ints(A), _ints(B), _ints(grid)))
+        spec = "packed:" + "|".join(dims)
+        pitch = O.pitch_of(P, spec)
+        assert d.extent() == pitch
+        want = O.global_offsets(P, spec, pitch, shape)
+        for g in np.ndindex(*shape):
+            assert d.global_offset(list(g), pitch) == want[g], (spec, g)
+
+
+def test_clone_dim_decomp():
+    """cloneDimDecomp copies a decorated DimDecomp: the clone lays out a decomposition identically and
+    outlives the original."""
+    lib = load()
+    P = 4
+    c = api.Comm(P)
+    orig = lib.makeRotatedDecomp(5, lib.makeFactorReverseDecomp(4, 3, lib.makeBlockDecomp(12, 2)))
+    clone = lib.cloneDimDecomp(orig)
+    assert lib.sizeDimDecomp(clone) == lib.sizeDimDecomp(orig) == 12
+    lib.freeDimDecomp(orig)
+    d = api.Decomp(c, lib.makePackedDecomp(c.h, 2, (ctypes.c_void_p * 2)(clone, lib.makeBlockDecomp(8, 2))))
+    spec = "packed:rotate(5,frev(4,3,block(12,2)))|block(8,2)"
+    pitch = O.pitch_of(P, spec)
+    want = O.global_offsets(P, spec, pitch, (12, 8))
+    for g in np.ndindex(12, 8):
+        assert d.global_offset(list(g), pitch) == want[g]
