@@ -1,6 +1,7 @@
 """The reference's smaller C entry points through the C-ABI, against the reference's semantics and the
 oracle (no GPU): run-length index sets, the locality and offset queries of a descriptor's view rank,
-the stage decompositions of the split FFT, and DimDecomp cloning."""
+the stage decompositions of the split FFT, DimDecomp cloning, the global-order decomposition and the
+stream setting."""
 import ctypes
 
 import numpy as np
@@ -113,3 +114,27 @@ def test_clone_dim_decomp():
     want = O.global_offsets(P, spec, pitch, (12, 8))
     for g in np.ndindex(12, 8):
         assert d.global_offset(list(g), pitch) == want[g]
+
+
+def test_global_decomp_is_c_order_on_rank_zero():
+    """dmg_makeGlobalDecomp: every element on rank 0, at its C-order linear index."""
+    lib = load()
+    c = api.Comm(4)
+    shape = (5, 3, 4)
+    d = api.Decomp(c, lib.dmg_makeGlobalDecomp(c.h, 3, _ints(shape)))
+    assert d.extent() == 60
+    for i, g in enumerate(np.ndindex(*shape)):
+        assert d.owner(list(g)) == 0
+        assert d.global_offset(list(g), 60) == i
+
+
+def test_stream_setting():
+    """dmg_set_stream / dmg_get_stream: the stream the reference-signature runs enqueue on (no CUDA call)."""
+    lib = load()
+    before = lib.dmg_get_stream()
+    try:
+        lib.dmg_set_stream(ctypes.c_void_p(0x1234))
+        assert lib.dmg_get_stream() == 0x1234
+    finally:
+        lib.dmg_set_stream(ctypes.c_void_p(before))
+    assert lib.dmg_get_stream() == before
