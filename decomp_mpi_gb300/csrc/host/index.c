@@ -2,6 +2,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include "dmg_internal.h"
 #include "index.h"
 
 Index makeIndex(void) {
@@ -33,8 +34,14 @@ void addIndex(Index ix, int offset) {
   }
   if (ix->count == ix->size) {
     int nsize = ix->size * 2;
-    ix->offsets = (int *)realloc(ix->offsets, (size_t)nsize * sizeof(int));
-    ix->counts = (int *)realloc(ix->counts, (size_t)nsize * sizeof(int));
+    int *no = (int *)realloc(ix->offsets, (size_t)nsize * sizeof(int));
+    if (no) ix->offsets = no;
+    int *nc = no ? (int *)realloc(ix->counts, (size_t)nsize * sizeof(int)) : NULL;
+    if (nc) ix->counts = nc;
+    if (!no || !nc) {
+      dmg_error(DMG_ERR_NOMEM, "addIndex: out of host memory (%d runs)", ix->count);
+      return; /* the index keeps its runs; the offset is not added */
+    }
     ix->size = nsize;
   }
   ix->offsets[ix->count] = offset;

@@ -165,6 +165,7 @@ static int layout_build(fft_layout *l, Decomp D, long long pitch, const char *wh
     int L = dd->coord_size;
     l->rk[d] = (int32_t *)malloc((size_t)L * sizeof(int32_t));
     l->tab[d] = (int64_t *)malloc((size_t)L * sizeof(int64_t));
+    if (!l->rk[d] || !l->tab[d]) return dmg_error(DMG_ERR_NOMEM, "split plan: out of host memory");
     for (int x = 0; x < L; ++x) {
       int p = dd->rank_offset(dd, x);
       int off = dd->type_offset(dd, x);
@@ -178,6 +179,7 @@ static int layout_build(fft_layout *l, Decomp D, long long pitch, const char *wh
   if (l->ranked) {
     int P = l->nranks;
     l->rstride = (int64_t *)malloc((size_t)nd * P * sizeof(int64_t));
+    if (!l->rstride) return dmg_error(DMG_ERR_NOMEM, "split plan: out of host memory");
     for (int d = 0; d < nd; ++d)
       for (int r = 0; r < P; ++r) l->rstride[(size_t)d * P + r] = dmg_axis_stride(D->dims[d], r);
   }
@@ -447,6 +449,7 @@ static int impl_upload(struct dmg_split_impl *im) {
   for (int d = 0; d < nd; ++d) bytes += align256((size_t)im->L[d] * cs);
   bytes += 256; /* scale exponent */
   char *host = (char *)calloc(1, bytes + 256);
+  if (!host) return dmg_error(DMG_ERR_NOMEM, "split plan: out of host memory for the device tables");
   void *dev = NULL;
   int st = dmg_dev_alloc(&dev, bytes + 256);
   if (st != DMG_OK) {
