@@ -307,3 +307,35 @@ def test_cuda_graph_replay_matches_eager(dtype, cuda):
         g2.replay()
         torch.cuda.synchronize()
         assert np.array_equal(r.dat.cpu().numpy(), want_back)
+
+
+@pytest.mark.skip(reason="written before its first GB300 run; enabled once it has passed there")
+def test_autotune_small_cube(cuda):
+    """autotuneParallelPlan (reference split_fft.c:78-247) on an 8x12x16 complex128 cube over a 2x2 grid:
+    it returns one of the makeParallelPlan plans in one of the two pass schedules; its forward transform
+    is the oracle's spectrum in that plan's slots, and has the same bits as makeParallelPlan with its
+    factors and schedule."""
+    import torch
+    P, spec, shape = 4, "packed:local(8)|block(12,2)|block(16,2)", (8, 12, 16)
+    comm = api.Comm(P)
+    S = api.decomp_from_spec(comm, spec)
+    dp, wl = S.extent(), 2 * int(np.prod(shape))
+    rng = np.random.default_rng(11)
+    glob = rng.uniform(-1, 1, shape) + 1j * rng.uniform(-1, 1, shape)
+    host = O.scatter_global(P, spec, glob, dp)
+    dat = torch.from_numpy(host).to(cuda)
+    work = torch.zeros(P * wl, dtype=torch.complex128, device=cuda)
+    stream = torch.cuda.current_stream(cuda).cuda_stream
+    sp = api.SplitPlan(S, dat.data_ptr(), wl, work.data_ptr(), autotune=True)
+    B = [L // a for L, a in zip(shape, sp.A_factors)]
+    dat.copy_(torch.from_numpy(host))  # the search ran forward transforms over the buffers
+    sp.run(api.FFTW_FORWARD, stream)
+    torch.cuda.synchronize()
+    got = work.cpu().numpy()
+    exp, mask = O.split_expected_output(P, spec, glob, wl, 2, B)
+    assert _rel(got[mask], exp[mask]) < TOL_C128
+    work2 = torch.zeros_like(work)
+    ref = api.SplitPlan(S, dat.data_ptr(), wl, work2.data_ptr(), B=B, schedule=sp.schedule)
+    ref.run(api.FFTW_FORWARD, stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(work2.cpu().numpy()[mask], got[mask])
