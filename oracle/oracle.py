@@ -99,7 +99,7 @@ def _ints(vals):
 # ---------------------------------------------------------------- oracle
 
 def decomp_info(P: int, spec: str):
-    """Per-rank extents and proc_used of a decomposition (oracle)."""
+    """Per-rank extents and proc_used of a decomposition (oracle; extent as reshape.c:47-324 computes it)."""
     ext = (ctypes.c_longlong * P)()
     pu = ctypes.c_int()
     rc = oracle_lib().oracle_decomp_info(P, spec.encode(), ext, ctypes.byref(pu))
@@ -114,7 +114,8 @@ def pitch_of(P: int, spec: str) -> int:
 
 
 def global_offsets(P: int, spec: str, pitch: int, shape) -> np.ndarray:
-    """Element offset of each global coordinate (C order) in the virtual-grid array; -1 when unheld."""
+    """Element offset of each global coordinate (C order) in the virtual-grid array; -1 when unheld
+    (rank r's buffer at r * pitch, getOffset of reshape.h:201 inside it)."""
     out = np.empty(int(np.prod(shape)), dtype=np.int64)
     rc = oracle_lib().oracle_global_offsets(P, spec.encode(), pitch, out.ctypes.data_as(_c_ll_p))
     if rc:
@@ -123,7 +124,8 @@ def global_offsets(P: int, spec: str, pitch: int, shape) -> np.ndarray:
 
 
 def reshape(P, src_spec, dst_spec, src: np.ndarray, src_pitch, dst: np.ndarray, dst_pitch, nthreads=8):
-    """Reshape src into dst (in place in dst) following the reference's message algorithm."""
+    """Reshape src into dst (in place in dst) following the reference's message algorithm
+    (makeReshapePlan / runReshapePlan, reshape.c:351-492; typemaps as typelist.c:74-119 builds them)."""
     assert src.dtype == dst.dtype and src.flags.c_contiguous and dst.flags.c_contiguous
     rc = oracle_lib().oracle_reshape(P, src_spec.encode(), dst_spec.encode(), src.dtype.itemsize, src_pitch,
                                      dst_pitch, src.ctypes.data, dst.ctypes.data, nthreads)
@@ -153,13 +155,15 @@ class ReshapePlanCPU:
 
 
 def processor_grid(P: int, tasks):
+    """makeProcessorGrid (processor_grid.c:73-97) restated by the oracle."""
     g = (ctypes.c_int * len(tasks))()
     oracle_lib().oracle_processor_grid(P, len(tasks), _ints(tasks), g)
     return list(g)
 
 
 def split_factors(P: int, start_spec: str, mode: int = 0, B=None):
-    """(A, B, grid_a, grid_b, a_spec, b_spec) of the split plan the reference would build."""
+    """(A, B, grid_a, grid_b, a_spec, b_spec) of the split plan the reference would build
+    (makeSplitPlan / makeParallelPlan, split_fft.c:570-614 and 747-788)."""
     nd = start_spec.count("|") + 1
     A = (ctypes.c_int * nd)()
     Bo = (ctypes.c_int * nd)()
@@ -175,7 +179,7 @@ def split_factors(P: int, start_spec: str, mode: int = 0, B=None):
 
 
 class SplitPlanCPU:
-    """Planned oracle split FFT (the reference's algorithm on CPU threads)."""
+    """Planned oracle split FFT (the reference's algorithm on CPU threads: runSplitPlan, split_fft.c:622-744)."""
 
     def __init__(self, P, start_spec, work_len, mode=0, B=None):
         nd = start_spec.count("|") + 1
@@ -262,7 +266,8 @@ def scatter_global(P, spec, glob: np.ndarray, pitch, fill=0):
 
 
 def split_expected_output(P, start_spec, glob_in: np.ndarray, work_len, mode=0, B=None):
-    """Expected forward split-FFT output: numpy FP64 fftn placed in the reference's B layout.
+    """Expected forward split-FFT output: numpy FP64 fftn placed in the reference's B layout
+    (the slots runSplitPlan's second stage writes, split_fft.c:690-700; getTransformed, split_fft.c:615-621).
 
     Global slot s_i = k2_i + A_i*k1_i of the B decomposition holds frequency
     k_i = k1_i + B_i*k2_i.  Returns (work array, mask of held slots).

@@ -52,6 +52,7 @@ static void search_grid(grid_best *best, int ndim, int mydim, int *grid, const i
   }
 }
 
+/* makeProcessorGrid (processor_grid.c:73-97): the search above from one task per rank upward */
 int oracle_processor_grid(int P, int ndim, const int *tasks, int *out) {
   grid_best b;
   b.length = (int *)calloc(ndim, sizeof(int));
@@ -168,6 +169,8 @@ static void twiddle_value(int y, int l, int L, double *re, double *im) {
   *im = s;
 }
 
+/* buildParallelPlan (split_fft.c:249-569): factors, grids, the A and B decompositions, their extents
+ * against the workspace (split_fft.c:304-308), and the twiddle tables */
 static int sp_build(splitplan *sp, int P, const char *start_spec, int mode, const int *Bin, long long work_len) {
   memset(sp, 0, sizeof(*sp));
   if (od_build(&sp->st, P, start_spec)) return -1;
@@ -227,6 +230,7 @@ static int sp_build(splitplan *sp, int P, const char *start_spec, int mode, cons
   return 0;
 }
 
+/* freeSplitPlan (split_fft.c:789-858) */
 static void sp_free(splitplan *sp) {
   for (int i = 0; i < sp->nd; ++i) {
     if (!sp->tw[i]) continue;
@@ -312,6 +316,7 @@ typedef struct {
   pthread_mutex_t mu;
 } stage_ctx;
 
+/* one virtual rank's batched FFTs of a stage (the fftw_execute calls of runSplitPlan, split_fft.c:638-690) */
 static void *stage_worker(void *arg) {
   stage_ctx *c = (stage_ctx *)arg;
   const splitplan *sp = c->sp;
@@ -343,6 +348,7 @@ static void *stage_worker(void *arg) {
   return NULL;
 }
 
+/* a stage over every rank, ranks spread over worker threads as the reference spreads them over processes */
 static void run_stage(const splitplan *sp, int stage, int sign, double *work, long long work_len, int nthreads) {
   stage_ctx c = {sp, stage, sign, work, work_len, 0};
   pthread_mutex_init(&c.mu, NULL);
@@ -356,6 +362,8 @@ static void run_stage(const splitplan *sp, int stage, int sign, double *work, lo
   pthread_mutex_destroy(&c.mu);
 }
 
+/* runSplitPlan (split_fft.c:622-744): forward = reshape start->A, stage-A FFTs, twiddle, reshape A->B,
+ * stage-B FFTs; the inverse runs those steps backwards with conjugate twiddles */
 static int sp_run(const splitplan *sp, long long dat_pitch, long long work_len, double *dat, double *work, int dir,
                   int nthreads) {
   int P = sp->P;
