@@ -3,6 +3,10 @@
  * Stockham (radices 4, 2, 3, 5 and a direct DFT for other primes) with
  * twiddles computed in long double.  Used by the FFTW guru-API stub that the
  * reference is built against, and by the CPU restatement of the split FFT.
+ * It stands in for FFTW 3, the third-party library the reference calls for
+ * its stages (fftw_plan_guru_dft / fftw_execute, split_fft.c:461-534 and
+ * 638-723; version not pinned by the reference, Makefile:7 links -lfftw3),
+ * with FFTW's conventions: sign -1 forward, unnormalised backward.
  */
 #ifndef ORACLE_CFFT_H
 #define ORACLE_CFFT_H
