@@ -5,7 +5,7 @@
  * reference is built against, and by the CPU restatement of the split FFT.
  * It stands in for FFTW 3, the third-party library the reference calls for
  * its stages (fftw_plan_guru_dft / fftw_execute, split_fft.c:461-534 and
- * 638-723; version not pinned by the reference, Makefile:7 links -lfftw3),
+ * 638-723; version not pinned by the reference, Makefile:8 links -lfftw3),
  * with FFTW's conventions: sign -1 forward, unnormalised backward.
  */
 #ifndef ORACLE_CFFT_H
