@@ -14,6 +14,8 @@ struct block_decomp {
 };
 typedef struct block_decomp *BlockDecomp;
 
+/** The plugin's hooks (reference block_decomp.h:13-14): rank and local offset of a
+ * global coordinate. */
 int block_rank_offset(DimDecomp d, int global);
 int block_type_offset(DimDecomp d, int global);
 /** Block decomposition of `len` coordinates over `proc` positions

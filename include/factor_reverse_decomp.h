@@ -17,6 +17,8 @@ struct factor_reverse_decomp {
 };
 typedef struct factor_reverse_decomp *FactorReverseDecomp;
 
+/** The plugin's hooks (reference factor_reverse_decomp.h:18-20): rank and local offset of a
+ * global coordinate, clone. */
 int factor_reverse_rank_offset(DimDecomp d, int global);
 int factor_reverse_type_offset(DimDecomp d, int global);
 DimDecomp clone_factor_reverse(DimDecomp d);

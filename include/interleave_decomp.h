@@ -18,6 +18,8 @@ struct interleave_decomp {
 };
 typedef struct interleave_decomp *InterleaveDecomp;
 
+/** The plugin's hooks (reference interleave_decomp.h:20-23): rank and local offset of a
+ * global coordinate, clone, print. */
 int interleave_rank_offset(DimDecomp d, int global);
 int interleave_type_offset(DimDecomp d, int global);
 void print_interleave(FILE *out, DimDecomp d);

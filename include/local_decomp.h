@@ -13,6 +13,8 @@ struct local_decomp {
 };
 typedef struct local_decomp *LocalDecomp;
 
+/** The plugin's hooks (reference local_decomp.h:11-13): rank and local offset of a
+ * global coordinate, clone. */
 int local_rank_offset(DimDecomp d, int global);
 int local_type_offset(DimDecomp d, int global);
 DimDecomp local_clone(DimDecomp d);

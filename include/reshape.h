@@ -65,6 +65,7 @@ void freeDimDecomp(DimDecomp);
 DimDecomp cloneDimDecomp(DimDecomp);
 /** Number of global coordinates (reference reshape.h:68). */
 int sizeDimDecomp(DimDecomp d);
+/** Print a DimDecomp through its print hook (reference reshape.h:67). */
 void describeDimDecomp(FILE *out, DimDecomp d);
 
 typedef struct axis_decomp *AxisDecomp;
@@ -100,6 +101,7 @@ Index makeGlobalIndex(AxisDecomp local);
 AxisDecomp makeAxisDecomp(MPI_Comm comm, DimDecomp d, int stride, int rank_stride);
 /** Free an AxisDecomp and its DimDecomp (reference reshape.h:122). */
 void freeAxisDecomp(AxisDecomp);
+/** Print an AxisDecomp (reference reshape.h:122). */
 void describeAxisDecomp(FILE *out, AxisDecomp d);
 /** Is `global` local to the view rank along this axis (reference reshape.h:129). */
 int isLocal(AxisDecomp d, int global);
@@ -124,6 +126,7 @@ Decomp makePackedDecomp(MPI_Comm comm, int ndim, DimDecomp dims[]);
 void freeDecomp(Decomp d);
 /** Print a Decomp (reference spelling, reshape.h:160). */
 void describeDeomp(FILE *out, Decomp d);
+/** The same, spelled correctly. */
 void describeDecomp(FILE *out, Decomp d);
 /** Largest memory extent over the virtual ranks, in elements
  * (reference reshape.h:164).  This is the default per-rank pitch of a

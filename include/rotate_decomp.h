@@ -15,6 +15,8 @@ struct rotate_decomp {
 };
 typedef struct rotate_decomp *RotateDecomp;
 
+/** The plugin's hooks (reference rotate_decomp.h:10-12): rank and local offset of a
+ * global coordinate, clone. */
 int rotate_rank_offset(DimDecomp d, int global);
 int rotate_type_offset(DimDecomp d, int global);
 DimDecomp clone_rotate(DimDecomp d);

@@ -14,6 +14,8 @@ struct single_decomp {
 };
 typedef struct single_decomp *SingleDecomp;
 
+/** The plugin's hooks (reference single_decomp.h:14-16): rank and local offset of a
+ * global coordinate, clone. */
 int single_rank_offset(DimDecomp d, int global);
 int single_type_offset(DimDecomp d, int global);
 DimDecomp single_clone(DimDecomp d);

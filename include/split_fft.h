@@ -111,6 +111,8 @@ Decomp getTransformedExact(SplitPlan plan);
 /** Run forward (FFTW_FORWARD) or inverse (FFTW_BACKWARD) on the current
  * stream (reference split_fft.h:60). */
 void runSplitPlan(SplitPlan plan, int direction);
+/** Free a plan with its decompositions and device tables; the caller's
+ * dat and workspace stay (reference split_fft.h:60). */
 void freeSplitPlan(SplitPlan plan);
 /** Interleaved decomposition: interleave(block(A_i, grid_i), B_i) packed
  * (reference split_fft.h:62). */
@@ -143,6 +145,7 @@ SplitPlan dmg_makeParallelPlanTyped(Decomp start, int *initial_factor, void *dat
 /** Select the arithmetic of a plan (DMG_ARITH_FP64 or DMG_ARITH_DF for
  * complex128; complex64 plans accept only DMG_ARITH_FP32). */
 int dmg_split_set_arith(SplitPlan plan, int arith);
+/** The arithmetic a plan computes in (DMG_ARITH_*). */
 int dmg_split_get_arith(SplitPlan plan);
 /* Pass schedule.  Both give the reference's output in the same workspace
  * slots.  LINES: one pass per dimension transforms all L_d points at once
