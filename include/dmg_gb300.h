@@ -35,6 +35,7 @@ void dmg_set_error_printing(int on);
 /* ---- streams ---- */
 /** Set the stream that run calls without an explicit stream use (this thread). */
 void dmg_set_stream(void *stream);
+/** The stream set by dmg_set_stream on this thread (NULL: the default stream). */
 void *dmg_get_stream(void);
 /** cudaDeviceSynchronize; returns DMG_OK or DMG_ERR_CUDA. */
 int dmg_device_synchronize(void);

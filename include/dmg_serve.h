@@ -63,6 +63,8 @@ int dmg_server_poll(DmgServer s, dmg_job_done *done, int max);
 int dmg_server_drain(DmgServer s);
 /** Jobs queued, running, and arena bytes in use. */
 int dmg_server_status(DmgServer s, int *queued, int *running, long long *arena_used);
+/** Finish the queued and running jobs, stop the scheduler thread and free
+ * the arena, the streams and the cached plans. */
 void dmg_server_destroy(DmgServer s);
 
 #ifdef __cplusplus
