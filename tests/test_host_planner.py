@@ -212,3 +212,34 @@ def test_factor_reverse_axis_decomp(A, B):
     want = O.global_offsets(P, spec, pitch, (12, 8))
     for g in np.ndindex(12, 8):
         assert D.global_offset(list(g), pitch) == want[g]
+
+
+def _bench_module():
+    import importlib.util
+    import os
+    spec = importlib.util.spec_from_file_location(
+        "bench_specs", os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "bench.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    return m
+
+
+@pytest.mark.parametrize("es", [16, 8, 4, 1])
+def test_measured_reshapes_plan_direct_16_byte_moves(es):
+    """The reshapes that are measured (the 512^3 chain on 8x8 and the sweep's transitions) plan onto
+    separable address tables with 16-byte moves (elements narrower than 16 bytes fused along the
+    contiguous axis): the kernel form that runs near the HBM copy rate."""
+    bench = _bench_module()
+    c = api.Comm(64)
+    D = [api.decomp_from_spec(c, s) for s in bench.specs(512)]
+    plans = [api.ReshapePlan(c, es, D[0], D[1]), api.ReshapePlan(c, es, D[1], D[2])]
+    for shape, g in [((256, 256, 256), 16), ((1024, 1024, 512), 32)]:
+        cg = api.Comm(g * g)
+        blk, other = bench.sweep_specs(shape, g)
+        S = api.decomp_from_spec(cg, blk)
+        for spec in other.values():
+            O_ = api.decomp_from_spec(cg, spec)
+            plans += [api.ReshapePlan(cg, es, S, O_), api.ReshapePlan(cg, es, O_, S)]
+    for p in plans:
+        d = p.describe()
+        assert d.startswith("src=separable dst=separable unit=%dB fuse=%d " % (es, 16 // es)), d
