@@ -162,3 +162,24 @@ def test_build_parallel_plan_explicit_grids():
         own_b.setdefault(x[:2], set()).add(B.owner(list(x)))
     assert all(len(v) == 1 for v in own_a.values()) and all(len(v) == 1 for v in own_b.values())
     assert set().union(*own_a.values()) == set().union(*own_b.values()) == {0, 1, 2, 3}
+
+
+@pytest.mark.parametrize("dtype", [api.C128, api.C64], ids=["c128", "c64"])
+def test_measured_split_plan_form(dtype):
+    """The measured 512^3 transform on the 8x8 grid (factor_reverse start, workspace twice the extent)
+    plans three one-pass-per-dimension passes of compile-time length 512 whose sides all take the
+    separable walks (orders tab / atb / abt, no per-value layout evaluation)."""
+    import re
+    c = api.Comm(64)
+    n = 512
+    spec = "packed:frev(16,32,block(%d,8))|frev(32,16,block(%d,8))|local(%d)" % (n, n, n)
+    S = api.decomp_from_spec(c, spec)
+    probe = api.SplitPlan(S, 1 << 20, 1 << 40, 1 << 21, dtype=dtype)
+    length = 2 * probe.extent
+    probe.free()
+    d = api.SplitPlan(S, 1 << 20, length, 1 << 21, dtype=dtype).describe()
+    assert " lines passes=3:" in d, d
+    passes = re.findall(r"\[d=(\d) n=(\d+) [^\]]* in=(\w+) out=(\w+)\]", d)
+    assert [(p[0], p[1]) for p in passes] == [("2", "512"), ("1", "512"), ("0", "512")], d
+    assert [(p[2], p[3]) for p in passes] == [("tab", "tab"), ("atb", "atb"), ("abt", "abt")], d
+    assert "per value" not in d and "shared dim" not in d, d
