@@ -44,7 +44,8 @@ class _DecompStruct(ctypes.Structure):
 
 
 class Comm:
-    """Virtual communicator of ``nranks`` virtual ranks (replaces MPI_Comm)."""
+    """Virtual communicator of ``nranks`` virtual ranks (replaces the MPI_Comm that reshape.h:77 keeps in
+    every AxisDecomp)."""
 
     def __init__(self, nranks: int):
         self.lib = load()
@@ -168,7 +169,7 @@ class _SpecParser:
 
 
 class Decomp:
-    """An N-D decomposition (owns its C handle)."""
+    """An N-D decomposition, the reference's Decomp (reshape.h:134-142; owns its C handle)."""
 
     def __init__(self, comm: Comm, handle):
         if not handle:
@@ -256,7 +257,7 @@ def decomp_from_spec(comm: Comm, spec: str) -> Decomp:
 
 
 class ReshapePlan:
-    """makeReshapePlan / runReshapePlan on the virtual grid."""
+    """makeReshapePlan / runReshapePlan (reshape.h:272-301, reshape.c:351-492) on the virtual grid."""
 
     def __init__(self, comm: Comm, elem_bytes: int, src: Decomp, dest: Decomp):
         self.lib = load()
@@ -317,7 +318,7 @@ def _int_array(vals):
 
 
 def processor_grid(comm: Comm, tasks):
-    """makeProcessorGrid: the reference's grid search over the communicator's ranks."""
+    """makeProcessorGrid (processor_grid.c:73-97): the reference's grid search over the communicator's ranks."""
     lib = load()
     ptr = lib.makeProcessorGrid(comm.h, len(tasks), _int_array(tasks))
     if not ptr:
@@ -348,7 +349,7 @@ class _BorrowedDecomp(Decomp):
 
 
 class SplitPlan:
-    """Split 3D FFT plan (makeSplitPlan / makeParallelPlan / autotuneParallelPlan).
+    """Split 3D FFT plan (makeSplitPlan / makeParallelPlan / autotuneParallelPlan, split_fft.h:10-63).
 
     ``dat`` and ``work`` are device pointers; ``length`` is the per-rank
     workspace length in elements.  ``dtype`` is C128 (FP64) or C64 (FP32).
@@ -524,7 +525,8 @@ def build_parallel_plan(flags: int, use_first: int, use_second: int, start: Deco
 # ---------------------------------------------------------------- global-order I/O
 
 def io_view(decomp: "Decomp", rank: int):
-    """makeIOType's file view for one rank: (file positions, buffer offsets) of its elements in C order."""
+    """makeIOType's file view (reshape.c:137-172) for one rank: (file positions, buffer offsets) of its
+    elements in C order."""
     import numpy as np
     lib = load()
     n = lib.dmg_io_view(decomp.h, int(rank), None, None, 0)
@@ -564,8 +566,9 @@ def read_file(path: str, decomp: "Decomp", elem_size: int, dst_ptr: int, stream=
 # ---------------------------------------------------------------- device visitors
 
 def decomp_scale(decomp: "Decomp", complex64: bool, data_ptr: int, factors, sign: int = -1, stream=None):
-    """dmg_decomp_scale: data *= prod_d factors[d][x_d] (conjugated for sign == 1); factors[d] a complex numpy
-    array of length L_d (complex128, or complex64 when complex64) or None."""
+    """dmg_decomp_scale, the device form of decomp_scale (dimscale.c:7-67): data *= prod_d factors[d][x_d]
+    (conjugated for sign == 1); factors[d] a complex numpy array of length L_d (complex128, or complex64 when
+    complex64) or None."""
     import numpy as np
     keep = []
     arr = (ctypes.c_void_p * 3)()

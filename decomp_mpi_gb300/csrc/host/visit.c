@@ -1,7 +1,8 @@
 /*
- * Device visitors (include/dmg_visit.h): the distributed array is gathered
- * to global C order with the K1 permutation kernel, visited element-wise,
- * and scattered back.  Three passes over the array instead of one, which is
+ * Device visitors (include/dmg_visit.h), the device forms of decomp_scale
+ * (reference dimscale.c:7-67) and of test.c:27's index fill: the
+ * distributed array is gathered to global C order with the K1 permutation
+ * kernel, visited element-wise, and scattered back.  Three passes over the array instead of one, which is
  * fine for initialisation and occasional scaling; the split FFT does not
  * use these (its twiddle is fused into the passes).
  */

@@ -1,5 +1,6 @@
 // Entry points of the FFT passes (dispatch by arithmetic) and the exponent
-// pre-pass of double-float runs.
+// pre-pass of double-float runs.  The passes are the execution of
+// runSplitPlan (reference split_fft.c:622-744).
 #include "fft_pass.cuh"
 
 // per-arithmetic launchers (fft_pass_f64.cu, fft_pass_f32.cu, fft_pass_df.cu)

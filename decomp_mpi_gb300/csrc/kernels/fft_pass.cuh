@@ -3,7 +3,9 @@
 // group of lengths).
 //
 // One launch transforms every line along one axis and writes the result in
-// another layout.  A block owns tiles of n x M1 x M2 values, persistent over
+// another layout: one pass does the work of a reshape (runReshapePlan), a
+// batch of FFTW transforms and the twiddle (decomp_scale) of the reference's
+// runSplitPlan (split_fft.c:622-744).  A block owns tiles of n x M1 x M2 values, persistent over
 // the tiles, in a three-buffer pipeline: the gather copies tile i+1 from the
 // input layout into a staging buffer with asynchronous copies (cp.async, in
 // the order contiguous in the input) while tile i goes through its Stockham

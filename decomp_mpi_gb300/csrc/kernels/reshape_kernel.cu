@@ -1,4 +1,6 @@
-// Reshape permutation kernel.
+// Reshape permutation kernel: the data movement of runReshapePlan
+// (reference reshape.c:461-492), whose per-peer typemaps (typelist.c:74-119)
+// and MPI exchange become one permutation over the virtual grid.
 //
 // One launch moves a whole virtual-grid array from one decomposition to
 // another: dst[addr_dst(g)] = src[addr_src(g)] for every global coordinate g

@@ -1,5 +1,6 @@
 // Element-wise kernels over a distributed array gathered to global C order
-// (the device visitors of include/dmg_visit.h).
+// (the device visitors of include/dmg_visit.h): the scaling of decomp_scale
+// (reference dimscale.c:7-67) and the index pattern of test.c:27.
 #include <cuda_runtime.h>
 #include <cstdint>
 #include "../host/dmg_internal.h"
