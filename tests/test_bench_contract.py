@@ -27,3 +27,15 @@ def test_reference_arm_line():
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
     assert d["cpu_baseline"]["kind"] in ("port", "reference") and d["cpu_baseline"]["cores"] >= 1
     assert "workload" in d["config"]
+
+
+@pytest.mark.timeout(120)
+def test_reference_arm_other_ranks_exit_quietly():
+    """Under torchrun with N > 1, ranks other than 0 leave the reference arm at once with status 0 and
+    print nothing; rank 0 alone runs and prints the line."""
+    env = dict(os.environ, RANK="1", WORLD_SIZE="2", LOCAL_RANK="1")
+    p = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2",
+                        "--steps", "1", "--warmup", "3"], capture_output=True, text=True, cwd=ROOT, env=env,
+                       timeout=120)
+    assert p.returncode == 0, p.stderr[-2000:]
+    assert not [ln for ln in p.stdout.splitlines() if ln.startswith("{")]
