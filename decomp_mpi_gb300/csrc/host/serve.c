@@ -21,80 +21,19 @@
 #include "block_decomp.h"
 #include "dmg_gb300.h"
 #include "dmg_internal.h"
+#include "arena.h"
 #include "dmg_serve.h"
 #include "fft_params.h"
 #include "local_decomp.h"
 #include "rotate_decomp.h"
 
-#define ALIGN 256
+#define ALIGN DMG_ARENA_ALIGN
 #define BYPASS 8 /* younger jobs that may start ahead of a head that does not fit */
 
 static double now_s(void) {
   struct timespec ts;
   clock_gettime(CLOCK_MONOTONIC, &ts);
   return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
-}
-
-/* ---------------------------------------------------------------- arena: first fit over one allocation */
-
-typedef struct {
-  long long off, size;
-} blk;
-
-typedef struct {
-  long long size, used;
-  blk *free;
-  int nfree, cap;
-} arena;
-
-static long long round_up(long long x) { return (x + ALIGN - 1) / ALIGN * ALIGN; }
-
-static long long arena_alloc(arena *a, long long bytes) {
-  bytes = round_up(bytes > 0 ? bytes : 1);
-  for (int i = 0; i < a->nfree; ++i) {
-    if (a->free[i].size >= bytes) {
-      long long off = a->free[i].off;
-      a->free[i].off += bytes;
-      a->free[i].size -= bytes;
-      if (a->free[i].size == 0) {
-        memmove(&a->free[i], &a->free[i + 1], (size_t)(a->nfree - i - 1) * sizeof(blk));
-        a->nfree--;
-      }
-      a->used += bytes;
-      return off;
-    }
-  }
-  return -1;
-}
-
-static int arena_free(arena *a, long long off, long long bytes) {
-  bytes = round_up(bytes > 0 ? bytes : 1);
-  int i = 0;
-  while (i < a->nfree && a->free[i].off < off) ++i;
-  if (a->nfree == a->cap) {
-    int nc = a->cap ? 2 * a->cap : 16;
-    blk *nb = (blk *)realloc(a->free, (size_t)nc * sizeof(blk));
-    if (!nb) return DMG_ERR_NOMEM;
-    a->free = nb;
-    a->cap = nc;
-  }
-  memmove(&a->free[i + 1], &a->free[i], (size_t)(a->nfree - i) * sizeof(blk));
-  a->free[i].off = off;
-  a->free[i].size = bytes;
-  a->nfree++;
-  /* coalesce with the neighbours */
-  if (i + 1 < a->nfree && a->free[i].off + a->free[i].size == a->free[i + 1].off) {
-    a->free[i].size += a->free[i + 1].size;
-    memmove(&a->free[i + 1], &a->free[i + 2], (size_t)(a->nfree - i - 2) * sizeof(blk));
-    a->nfree--;
-  }
-  if (i > 0 && a->free[i - 1].off + a->free[i - 1].size == a->free[i].off) {
-    a->free[i - 1].size += a->free[i].size;
-    memmove(&a->free[i], &a->free[i + 1], (size_t)(a->nfree - i - 1) * sizeof(blk));
-    a->nfree--;
-  }
-  a->used -= bytes;
-  return DMG_OK;
 }
 
 /* ---------------------------------------------------------------- plans */
@@ -417,13 +356,8 @@ DmgServer dmg_server_create(int grid, long long arena_bytes, int slots, int max_
   void *base = NULL;
   if (dmg_dev_alloc(&base, (size_t)arena_bytes) != DMG_OK) goto fail;
   s->base = (char *)base;
-  s->ar.size = arena_bytes / ALIGN * ALIGN; /* what the free list can hand out: a job larger never fits */
-  s->ar.cap = 16;
-  s->ar.free = (blk *)calloc(16, sizeof(blk));
-  if (!s->ar.free) goto fail;
-  s->ar.free[0].off = 0;
-  s->ar.free[0].size = arena_bytes / ALIGN * ALIGN;
-  s->ar.nfree = 1;
+  /* the capacity is what the free list can hand out: a larger job never fits */
+  if (arena_init(&s->ar, arena_bytes) != DMG_OK) goto fail;
   s->slots = (slot *)calloc((size_t)slots, sizeof(slot));
   if (!s->slots) goto fail;
   for (int i = 0; i < slots; ++i)
@@ -545,7 +479,7 @@ void dmg_server_destroy(DmgServer s) {
     }
     free(s->slots);
   }
-  free(s->ar.free);
+  arena_release(&s->ar);
   if (s->base) dmg_dev_free(s->base);
   if (s->comm) dmg_comm_free(s->comm);
   free(s);
