@@ -28,7 +28,7 @@ SIGNATURES = {
     "dmg_last_error": (_cp, []),
     "dmg_last_error_code": (_i, []),
     "dmg_clear_error": (None, []),
-    "dmg_set_error_printing": (None, [_i]),
+    "dmg_set_error_printing": (_i, [_i]),
     "dmg_set_stream": (None, [_vp]),
     "dmg_get_stream": (_vp, []),
     "dmg_device_synchronize": (_i, []),

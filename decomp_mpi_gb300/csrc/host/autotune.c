@@ -134,9 +134,9 @@ SplitPlan dmg_autotune_split(Decomp start, void *dat, long long length, void *wo
   tune_ctx c = {start, dat, workspace, length, dtype, full_grid_search, NULL, 1e30, NULL, 0};
   c.ev = dmg_split_create_events(2);
   int B[DMG_MAXAX] = {0};
-  dmg_set_error_printing(0);
+  const int printing = dmg_set_error_printing(0);
   factors(&c, start->ndim, 0, B);
-  dmg_set_error_printing(1);
+  dmg_set_error_printing(printing);
   dmg_split_destroy_events(c.ev);
   if (!c.best) dmg_error(DMG_ERR_ARG, "autotune: no candidate plan could be built");
   else dmg_clear_error();

@@ -7,7 +7,7 @@
 
 static _Thread_local char g_err_msg[512];
 static _Thread_local int g_err_code = DMG_OK;
-static int g_err_print = 1;
+static _Thread_local int g_err_print = 1;
 
 int dmg_error(int code, const char *fmt, ...) {
   va_list ap;
@@ -25,7 +25,11 @@ void dmg_clear_error(void) {
   g_err_code = DMG_OK;
   g_err_msg[0] = 0;
 }
-void dmg_set_error_printing(int on) { g_err_print = on; }
+int dmg_set_error_printing(int on) {
+  const int prev = g_err_print;
+  g_err_print = on;
+  return prev;
+}
 
 /* The reference prints "<rank>: Error in reshape:<msg>" and aborts with
  * code 555 (reshape.c:12-21).  Here the message becomes the thread's last

@@ -29,8 +29,9 @@ const char *dmg_last_error(void);
 int dmg_last_error_code(void);
 /** Clear this thread's error. */
 void dmg_clear_error(void);
-/** Print errors to stderr when they are recorded (default on). */
-void dmg_set_error_printing(int on);
+/** Print this thread's errors to stderr when they are recorded (default
+ * on); returns the previous setting. */
+int dmg_set_error_printing(int on);
 
 /* ---- streams ---- */
 /** Set the stream that run calls without an explicit stream use (this thread). */

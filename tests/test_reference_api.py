@@ -138,3 +138,19 @@ def test_stream_setting():
     finally:
         lib.dmg_set_stream(ctypes.c_void_p(before))
     assert lib.dmg_get_stream() == before
+
+
+def test_error_printing_switch_is_per_thread():
+    """dmg_set_error_printing returns the previous setting and applies to the calling thread only."""
+    import threading
+    lib = load()
+    prev = lib.dmg_set_error_printing(0)
+    try:
+        seen = []
+        t = threading.Thread(target=lambda: seen.append(lib.dmg_set_error_printing(1)))
+        t.start()
+        t.join()
+        assert seen == [1]  # a new thread starts with printing on
+        assert lib.dmg_set_error_printing(0) == 0  # this thread's setting was not touched by the other
+    finally:
+        lib.dmg_set_error_printing(prev)
