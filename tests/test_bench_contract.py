@@ -39,3 +39,34 @@ def test_reference_arm_other_ranks_exit_quietly():
                        timeout=120)
     assert p.returncode == 0, p.stderr[-2000:]
     assert not [ln for ln in p.stdout.splitlines() if ln.startswith("{")]
+
+
+def test_clock_sampler_parses_reasons_and_median():
+    """The clock record of the timed region: median SM clock under load, the maximum, and every throttle reason
+    seen active (nvidia-smi csv, noheader, nounits)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_clocks", os.path.join(ROOT, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+
+    class _Done:
+        def terminate(self):
+            pass
+
+        def wait(self, timeout=None):
+            return 0
+
+    s = bench.ClockSampler("0")
+    s.proc = _Done()
+    s.lines = [
+        "0, 1965, 2070, 900.1, 0x0, Not Active, Not Active, Not Active, Not Active",
+        "0, 1980, 2070, 1100.0, 0x4, Not Active, Not Active, Not Active, Active",
+        "0, 2010, 2070, 1200.5, 0x0, Not Active, Not Active, Not Active, Not Active",
+        "garbage line",
+    ]
+    r = s.stop()
+    assert r["sm_mhz"] == 1980 and r["sm_max_mhz"] == 2070 and r["samples"] == 3
+    assert r["reasons"] == ["sw_power_cap"]
+    s.lines.append("0, 1500, 2070, 1300.0, 0x8, Active, Not Active, Active, Not Active")
+    r = s.stop()
+    assert r["reasons"] == ["hw_slowdown", "sw_power_cap", "sw_thermal_slowdown"]
