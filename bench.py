@@ -899,10 +899,11 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--sweep", action="store_true", help="reshape bandwidth sweep (one JSON line per case)")
     ap.add_argument("--quick", action="store_true", help="with --sweep: the 256^3 shapes only")
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--gpus", type=int, default=1, help="replicas, one per GPU (under torch.distributed.run)")
+    ap.add_argument("--steps", type=int, default=10, help="timed steps")
+    ap.add_argument("--warmup", type=int, default=3, help="untimed steps before them (at least 3)")
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"],
+                    help="reference: the reference's algorithm on the host cores (the CPU restatement)")
     ap.add_argument("--n", type=int, default=N_SIDE, help="cube side (the headline workload is 512)")
     ap.add_argument("--fft", action="store_true", help="split FFT alone at --n: per-arithmetic, per-schedule times")
     ap.add_argument("--dtype", default="c128", choices=["c128", "c64"], help="with --fft: element type")
