@@ -392,7 +392,9 @@ int dmg_server_job_sizes(DmgServer s, int side, int dtype, long long *input, lon
 }
 
 long long dmg_server_submit(DmgServer s, const dmg_job *job) {
-  if (!s || !job || !job->input) return -dmg_error(DMG_ERR_ARG, "dmg_server_submit: bad job");
+  if (!s || !job || !job->input || job->side < 1 || (job->dtype != DMG_C128 && job->dtype != DMG_C64))
+    return -dmg_error(DMG_ERR_ARG, "dmg_server_submit: bad job (side %d, dtype %d)", job ? job->side : 0,
+                      job ? job->dtype : -1);
   job_rec *jr = (job_rec *)calloc(1, sizeof(job_rec));
   if (!jr) return -dmg_error(DMG_ERR_NOMEM, "dmg_server_submit: out of memory");
   jr->j = *job;
