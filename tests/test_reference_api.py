@@ -154,3 +154,19 @@ def test_error_printing_switch_is_per_thread():
         assert lib.dmg_set_error_printing(0) == 0  # this thread's setting was not touched by the other
     finally:
         lib.dmg_set_error_printing(prev)
+
+
+@pytest.mark.parametrize("spec", ["packed:block(8,2", "packed:blok(8,2)", "cols:block(8,2)", "packed:block(8)",
+                                  "packed:", "packed:block(8,2)|", "axes:block(8,2)",
+                                  "packed:frev(3,3,block(8,2))", "packed:block(8,5)"])
+def test_bad_decomposition_specs_are_rejected(spec):
+    """Malformed spec strings and decompositions the constructors refuse (factors that do not multiply to
+    the length, a grid larger than the communicator) raise instead of returning a descriptor."""
+    c = api.Comm(4)
+    lib = load()
+    prev = lib.dmg_set_error_printing(0)
+    try:
+        with pytest.raises((ValueError, api.DecompError)):
+            api.decomp_from_spec(c, spec)
+    finally:
+        lib.dmg_set_error_printing(prev)
