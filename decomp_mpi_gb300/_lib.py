@@ -103,7 +103,6 @@ SIGNATURES = {
     "dmg_split_set_timing": (_i, [_vp, _i]),
     "dmg_split_collect_times": (_i, [_vp]),
     "dmg_split_pass_times": (_i, [_vp, _i, ctypes.POINTER(ctypes.c_float), _i]),
-    "dmg_probe_fma_tflops": (ctypes.c_double, [_i]),
     "dmg_split_run_noalloc": (_i, [_vp, _i, _vp]),
     "dmg_split_set_arith": (_i, [_vp, _i]),
     "dmg_split_get_arith": (_i, [_vp]),

@@ -61,12 +61,6 @@ const char *dmg_reshape_describe(ReshapePlan plan);
 /** Kernel launches one run makes. */
 int dmg_reshape_launches(ReshapePlan plan);
 
-/* ---- diagnostics ---- */
-/** FMA throughput of the current GPU in TFLOP/s (an FMA is two flops),
- * measured by a short dependent-chain kernel: which = 0 FP64, 1 FP32.
- * Negative on error.  The FP64 rate bounds the FP64 FFT passes. */
-double dmg_probe_fma_tflops(int which);
-
 #ifdef __cplusplus
 }
 #endif

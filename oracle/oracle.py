@@ -19,7 +19,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libref.so")
-REF_SOURCES = os.environ.get("DMG_REFERENCE_DIR", "/root/reference")
+# the reference checkout, when one is present: DMG_REFERENCE_DIR names it (no default)
+REF_SOURCES = os.environ.get("DMG_REFERENCE_DIR", "")
 
 _c_ll = ctypes.c_longlong
 _c_ll_p = ctypes.POINTER(ctypes.c_longlong)
@@ -31,7 +32,7 @@ _cp = ctypes.c_char_p
 def build(ref: bool = True) -> None:
     """Compile the oracle restatement, and the reference library when its sources are present."""
     subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
-    if ref and os.path.isdir(REF_SOURCES):
+    if ref and REF_SOURCES and os.path.isdir(REF_SOURCES):
         subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + REF_SOURCES], check=True)
 
 
@@ -250,6 +251,18 @@ def ref_split(P, start_spec, dat: np.ndarray, dat_pitch, work_len, mode=0, B=Non
 
 # ---------------------------------------------------------------- FFT value oracle
 
+def fftn64(x: np.ndarray, inverse: bool = False) -> np.ndarray:
+    """FP64 n-dimensional DFT (forward sign -1, unnormalised) on the host: pocketfft through scipy on every
+    host core when scipy is present, numpy's pocketfft otherwise."""
+    x = np.asarray(x, dtype=np.complex128)
+    try:
+        import scipy.fft as sf
+        f = sf.ifftn if inverse else sf.fftn
+        return f(x, workers=os.cpu_count() or 1, norm="forward" if inverse else "backward")
+    except ImportError:
+        return np.fft.ifftn(x) * x.size if inverse else np.fft.fftn(x)
+
+
 def gather_global(P, spec, arr: np.ndarray, pitch, shape) -> np.ndarray:
     """Global array (C order) from a virtual-grid array."""
     off = global_offsets(P, spec, pitch, shape)
@@ -273,7 +286,7 @@ def split_expected_output(P, start_spec, glob_in: np.ndarray, work_len, mode=0, 
     k_i = k1_i + B_i*k2_i.  Returns (work array, mask of held slots).
     """
     A, Bf, ga, gb, a_spec, b_spec = split_factors(P, start_spec, mode, B)
-    F = np.fft.fftn(glob_in)
+    F = fftn64(glob_in)
     shape = glob_in.shape
     use_first = all(a == 1 for a in A)
     out_spec = a_spec if use_first else b_spec
