@@ -86,6 +86,7 @@ struct dmg_split_impl {
   size_t scratch_bytes;
   void *dev; /* one device allocation for every table */
   int dev_valid;
+  int dev_id; /* the CUDA device the tables were uploaded on */
   void *dat, *work;
   int timing;
   void *events;
@@ -433,9 +434,16 @@ static void fill_side(struct dmg_fft_layout *fl, const fft_layout *hl, int nd, i
   fl->base = base;
 }
 
+size_t dmg_noalloc_scratch_bytes(void);
+int dmg_noalloc_scratch(void **ptr);
+int dmg_noalloc_scratch_reserve(void);
+
 /* Upload layout, root and twiddle tables; point every pass at them. */
 static int impl_upload(struct dmg_split_impl *im) {
   impl_free_device(im);
+  int dev_id = 0;
+  int st0 = dmg_rt_get_device(&dev_id);
+  if (st0 != DMG_OK) return st0;
   int nd = im->ndim;
   size_t cs = im->dtype == DMG_C128 ? 16 : 8;
   size_t bytes = 0;
@@ -533,6 +541,7 @@ static int impl_upload(struct dmg_split_impl *im) {
   }
   im->dev = dev;
   im->dev_valid = 1;
+  im->dev_id = dev_id;
   for (int dir = 0; dir < 2; ++dir) {
     pass_rec *list = dir == 0 ? im->fwd : im->inv;
     int cnt = dir == 0 ? im->nfwd : im->ninv;
@@ -564,6 +573,12 @@ static int impl_upload(struct dmg_split_impl *im) {
       }
     }
   }
+  /* a plan small enough for dmg_split_run_noalloc: make the module that
+   * holds the fixed scratch array resident on this device now (modules load
+   * lazily, and loading one reserves its __device__ arrays), so that the
+   * no-allocation call finds the array in place instead of reserving it
+   * itself; if that fails here, that call reports the error */
+  if (im->scratch_bytes <= dmg_noalloc_scratch_bytes()) dmg_noalloc_scratch_reserve();
   return DMG_OK;
 }
 
@@ -1221,9 +1236,6 @@ int dmg_split_batch_launches(SplitPlan plan, int direction, int count) {
 
 /* ---------------------------------------------------------------- no-allocation run */
 
-size_t dmg_noalloc_scratch_bytes(void);
-int dmg_noalloc_scratch(void **ptr);
-
 /* runSplitPlan without touching the allocator: the intermediate passes live
  * in the library's fixed device scratch array instead of the upper half of
  * the workspace.  The plan's tables must already be on the device (one
@@ -1246,8 +1258,16 @@ int dmg_split_run_noalloc(SplitPlan plan, int direction, void *stream) {
     return dmg_error(DMG_ERR_ARG,
                      "dmg_split_run_noalloc: the plan's tables are not on the device yet; run it once with "
                      "runSplitPlan or dmg_split_run, which uploads them");
+  int cur = 0;
+  int st = dmg_rt_get_device(&cur);
+  if (st != DMG_OK) return st;
+  if (cur != im->dev_id)
+    return dmg_error(DMG_ERR_ARG,
+                     "dmg_split_run_noalloc: the plan's tables are on device %d but device %d is current; make "
+                     "device %d current for this call",
+                     im->dev_id, cur, im->dev_id);
   void *scratch = NULL;
-  int st = dmg_noalloc_scratch(&scratch);
+  st = dmg_noalloc_scratch(&scratch);
   if (st != DMG_OK) return st;
   pass_rec *list = direction == FFTW_FORWARD ? im->fwd_s : im->inv_s;
   int cnt = direction == FFTW_FORWARD ? im->nfwd : im->ninv;

@@ -196,24 +196,27 @@ int dmg_split_pass_times(SplitPlan plan, int direction, float *ms, int max);
 const char *dmg_split_describe(SplitPlan plan);
 
 /** runSplitPlan for callers that cannot allocate device memory when they
- * run the transform: code inside a region that a CUDA graph is capturing, a
- * real-time loop that must not wait on the allocator, or an application
- * that gives all of HBM to its own pool.  It has no counterpart in the
- * reference (whose MPI ranks always own their workspace).
+ * run the transform: a real-time loop that must not wait on the allocator,
+ * or an application that gives all of HBM to its own pool up front and so
+ * has nothing left for a library to cudaMalloc.  It has no counterpart in
+ * the reference (whose MPI ranks always own their workspace).
  *
- * The intermediate passes use a fixed device array of 64 MiB that the
- * library holds on every GPU it runs on until the process exits, instead of
+ * The intermediate passes use a fixed device array of 64 MiB instead of
  * the upper half of each rank's workspace; `dat` and the B-layout output in
  * the workspace's lower half are the caller's buffers as usual.  The call
- * allocates nothing: the plan's address tables must already be on the
- * device (any earlier dmg_split_run / runSplitPlan of the plan uploads
- * them, otherwise the call returns DMG_ERR_ARG), and plans needing more
- * than 64 MiB of scratch (virtual ranks x extent x element size) are
- * rejected with DMG_ERR_BOUNDS.  The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress); make that first call
- * before any stream capture.  Every call uses the same array and the
- * passes overwrite whatever an earlier call left there; calls that overlap
- * on the GPU (different streams, no ordering) race on it. */
+ * allocates nothing and makes no allocating library call:
+ *  - the plan's address tables must already be on the device: any earlier
+ *    dmg_split_run / runSplitPlan of the plan uploads them, otherwise the
+ *    call returns DMG_ERR_ARG;
+ *  - that upload also loads the array on the device (a device holds it from
+ *    then until the process exits), so the call finds it in place;
+ *  - the device the tables were uploaded on must be current, otherwise the
+ *    call returns DMG_ERR_ARG;
+ *  - plans needing more than 64 MiB of scratch (virtual ranks x extent x
+ *    element size) are rejected with DMG_ERR_BOUNDS before any device work.
+ * Every call uses the same array, and the passes overwrite whatever an
+ * earlier call left there; calls that overlap on the GPU (different
+ * streams, no ordering between them) race on it. */
 int dmg_split_run_noalloc(SplitPlan plan, int direction, void *stream);
 /** Size in bytes of the fixed scratch array used by dmg_split_run_noalloc. */
 size_t dmg_noalloc_scratch_bytes(void);
