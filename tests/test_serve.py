@@ -154,3 +154,57 @@ def test_server_refuses_a_job_larger_than_the_arena(cuda):
     with pytest.raises(RuntimeError):
         srv.submit(64, api.C128, x.data_ptr())
     srv.close()
+
+
+C5_SIDES = [48, 64, 96, 120, 128, 160, 192, 240, 256, 320, 384, 480, 512]
+
+
+def _check_job(srv, side, dtype, g, hs, ho):
+    """A served job's spectrum against the FP64 oracle (global frequency order) and its inverse against
+    N times the input."""
+    blk, rot = api.cube_specs(side, GRID)
+    shape = (side,) * 3
+    _, n_spec, n_out = srv.sizes(side, dtype)
+    ext = n_spec // P
+    A, Bf, _, _, _, b_spec = O.split_factors(P, rot)
+    got = hs.numpy()[O.global_offsets(P, b_spec, ext, shape)].astype(np.complex128)
+    F = O.fftn64(g)
+    k = [np.arange(side) // A[d] + Bf[d] * (np.arange(side) % A[d]) for d in range(3)]
+    want = F[np.ix_(*k)]
+    del F
+    e_spec = _rel(got, want)
+    del got, want
+    back = ho.numpy()[O.global_offsets(P, rot, n_out // P, shape)].astype(np.complex128) / side ** 3
+    e_back = _rel(back, g)
+    return e_spec, e_back
+
+
+@pytest.mark.parametrize("sides", [C5_SIDES[:9], [320], [384], [480], [512]],
+                         ids=["48-256", "320", "384", "480", "512"])
+def test_server_every_c5_side_both_types(sides, cuda):
+    """Every cube side of the served stream, in complex64 and complex128, through the server in one mix
+    (several slots, batching on): spectra against the FP64 oracle and inverses back to N times the
+    input, within 1e-12 (complex128) and 2e-6 (complex64)."""
+    import torch
+    jobs = [(s, dt, 1000 + 2 * s + dt) for s in sides for dt in (api.C128, api.C64)]
+    srv = api.Server(GRID, 32 << 30, slots=3, max_batch=8)
+    bufs = []
+    for side, dtype, seed in jobs:
+        blk, _ = api.cube_specs(side, GRID)
+        n_in, n_spec, n_out = srv.sizes(side, dtype)
+        g = _cube(side, dtype, seed)
+        pitch = n_in // P
+        hi = torch.from_numpy(O.scatter_global(P, blk, g, pitch)).pin_memory()
+        assert hi.numel() == n_in
+        hs = torch.zeros(n_spec, dtype=hi.dtype).pin_memory()
+        ho = torch.zeros(n_out, dtype=hi.dtype).pin_memory()
+        bufs.append((g, hi, hs, ho))
+        srv.submit(side, dtype, hi.data_ptr(), hs.data_ptr(), ho.data_ptr())
+    srv.drain()
+    done = srv.poll()
+    assert len(done) == len(jobs) and all(d["status"] == 0 for d in done)
+    for (side, dtype, _), (g, hi, hs, ho) in zip(jobs, bufs):
+        e_spec, e_back = _check_job(srv, side, dtype, g.astype(np.complex128), hs, ho)
+        assert e_spec < TOL[dtype], (side, dtype, e_spec)
+        assert e_back < TOL[dtype], (side, dtype, e_back)
+    srv.close()
