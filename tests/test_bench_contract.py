@@ -13,7 +13,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 @pytest.mark.timeout(600)
 def test_reference_arm_line():
     p = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
-                        "--warmup", "3"], capture_output=True, text=True, cwd=ROOT, timeout=600)
+                        "--warmup", "3", "--n", "128"], capture_output=True, text=True, cwd=ROOT, timeout=600)
     assert p.returncode == 0, p.stderr[-2000:]
     lines = [ln for ln in p.stdout.splitlines() if ln.startswith("{")]
     assert len(lines) == 1
@@ -26,7 +26,7 @@ def test_reference_arm_line():
     assert d["value"] > 0 and d["unit"] == "GFLOP/s" and d["higher_is_better"] is True
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
     assert d["cpu_baseline"]["kind"] in ("port", "reference") and d["cpu_baseline"]["cores"] >= 1
-    assert "workload" in d["config"]
+    assert "workload" in d["config"] and d["config"]["workload"].startswith("128^3")
 
 
 @pytest.mark.timeout(120)
