@@ -106,6 +106,7 @@ SIGNATURES = {
     "dmg_split_run_noalloc": (_i, [_vp, _i, _vp]),
     "dmg_split_set_arith": (_i, [_vp, _i]),
     "dmg_split_get_arith": (_i, [_vp]),
+    "dmg_split_device_status": (_i, [_vp]),
     "dmg_split_set_schedule": (_i, [_vp, _i]),
     "dmg_split_run_batch": (_i, [_vp, _i, _vp, _i, _vp, _vp, _vp]),
     "dmg_split_batch_launches": (_i, [_vp, _i, _i]),

@@ -28,6 +28,7 @@ C64 = 1
 ARITH_FP64 = 0
 ARITH_FP32 = 1
 ARITH_DF = 2
+ARITH_TC16 = 3
 SCHEDULE_AUTO = 0
 SCHEDULE_LINES = 1
 SCHEDULE_SPLIT = 2
@@ -380,8 +381,16 @@ class SplitPlan:
             self.set_schedule(schedule)
 
     def set_arith(self, arith):
-        """ARITH_DF (default for complex128) or ARITH_FP64; complex64 plans are ARITH_FP32."""
+        """ARITH_DF (default for complex128) or ARITH_FP64; ARITH_FP32 (default for complex64) or ARITH_TC16
+        (the 1024-point passes' DFTs on the tensor cores) for complex64."""
         check(self.lib.dmg_split_set_arith(self.h, int(arith)), "dmg_split_set_arith")
+
+    def device_status(self):
+        """0 when every tensor-core pass completed its products (reads the device word after the queued work)."""
+        st = self.lib.dmg_split_device_status(self.h)
+        if st < 0:
+            raise DecompError("dmg_split_device_status: %s" % last_error())
+        return st
 
     @property
     def arith(self):

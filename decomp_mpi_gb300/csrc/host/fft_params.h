@@ -86,6 +86,9 @@ struct dmg_fft_pass {
    * both axes make up */
   int32_t semi_in, semi_out, semi_a, semi_b;
   struct dmg_fft_layout in, out;
+  /* device word set to 1 when a tensor-core pass gave up waiting for its
+   * products (NULL: not reported) */
+  int32_t *status;
 };
 
 /* Threads per pass block; the most values a tile may hold, and the number
@@ -112,7 +115,9 @@ extern "C" {
  * share the persistent blocks). */
 int dmg_fft_pass_launch_batch(const struct dmg_fft_pass *p, int dtype, const struct dmg_fft_batch *b, void *stream);
 /* dtype 0: complex128 in FP64 arithmetic, 1: complex64 in FP32, 2: complex128
- * data in double-float (FP32 pair) arithmetic. */
+ * data in double-float (FP32 pair) arithmetic, 3: complex64 with the
+ * 1024-point passes' DFTs on the tensor cores (FP16 hi + lo operands, FP32
+ * accumulation; other lengths as dtype 1). */
 int dmg_fft_pass_launch(const struct dmg_fft_pass *p, int dtype, const void *src, void *dst, void *stream);
 /* Largest biased FP64 exponent of max(|re|, |im|) over the N = prod(L)
  * complex128 elements of a layout, into *out (which the call first sets to 0). */

@@ -65,6 +65,7 @@ struct dmg_split_impl {
   int dtype; /* DMG_C128 or DMG_C64 */
   int arith; /* DMG_ARITH_FP64, DMG_ARITH_DF (complex128) or DMG_ARITH_FP32 (complex64) */
   int32_t *d_scale; /* device int: largest input exponent (double-float runs) */
+  int32_t *d_status; /* device int: 1 when a tensor-core pass gave up waiting for its products */
   int esize; /* bytes per element */
   int ndim;
   int A[DMG_FFT_MAXDIM], B[DMG_FFT_MAXDIM], L[DMG_FFT_MAXDIM];
@@ -532,6 +533,7 @@ static int impl_upload(struct dmg_split_impl *im) {
     pos += align256((size_t)im->L[d] * cs);
   }
   im->d_scale = (int32_t *)((char *)dev + pos);
+  im->d_status = im->d_scale + 1; /* zero from the upload */
   pos += 256;
   st = dmg_dev_upload(dev, host, pos);
   free(host);
@@ -554,6 +556,7 @@ static int impl_upload(struct dmg_split_impl *im) {
       list[k].p.in_fp64 = im->arith == DMG_ARITH_DF && k == 0;
       list[k].p.out_fp64 = im->arith == DMG_ARITH_DF && k == cnt - 1;
       list[k].p.scale_exp = im->d_scale;
+      list[k].p.status = im->d_status;
       fill_side(&list[k].p.in, &im->lay[list[k].in_lay], nd, list[k].in_base);
       fill_side(&list[k].p.out, &im->lay[list[k].out_lay], nd, list[k].out_base);
       list[k].p.t0_rel_in = list[k].p.sep_in && t0_rel32(&im->lay[list[k].in_lay], &list[k].p);
@@ -774,7 +777,7 @@ static int build_passes(struct dmg_split_impl *im) {
 
 /* kernel dtype of a plan's arithmetic */
 static int arith_dtype(const struct dmg_split_impl *im) {
-  return im->arith == DMG_ARITH_FP64 ? 0 : im->arith == DMG_ARITH_FP32 ? 1 : 2;
+  return im->arith == DMG_ARITH_FP64 ? 0 : im->arith == DMG_ARITH_FP32 ? 1 : im->arith == DMG_ARITH_DF ? 2 : 3;
 }
 
 /* largest exponent of the run's complex128 input, for the double-float scaling */
@@ -1047,7 +1050,8 @@ int dmg_split_set_dat_pitch(SplitPlan plan, long long pitch) {
 int dmg_split_set_arith(SplitPlan plan, int arith) {
   if (!plan) return dmg_error(DMG_ERR_ARG, "dmg_split_set_arith: NULL plan");
   struct dmg_split_impl *im = plan->impl;
-  if (im->dtype == DMG_C64 ? arith != DMG_ARITH_FP32 : (arith != DMG_ARITH_FP64 && arith != DMG_ARITH_DF))
+  if (im->dtype == DMG_C64 ? (arith != DMG_ARITH_FP32 && arith != DMG_ARITH_TC16)
+                           : (arith != DMG_ARITH_FP64 && arith != DMG_ARITH_DF))
     return dmg_error(DMG_ERR_ARG, "dmg_split_set_arith: arithmetic %d does not apply to this element type", arith);
   if (arith != im->arith) {
     im->arith = arith;
@@ -1057,6 +1061,15 @@ int dmg_split_set_arith(SplitPlan plan, int arith) {
 }
 
 int dmg_split_get_arith(SplitPlan plan) { return plan ? plan->impl->arith : -1; }
+
+int dmg_split_device_status(SplitPlan plan) {
+  if (!plan) return -dmg_error(DMG_ERR_ARG, "dmg_split_device_status: NULL plan");
+  struct dmg_split_impl *im = plan->impl;
+  if (!im->dev_valid) return 0; /* nothing has run since the tables were (re)made */
+  int32_t v = 0;
+  int st = dmg_copy_sync(&v, im->d_status, sizeof(v), 1, NULL);
+  return st != DMG_OK ? -st : v;
+}
 
 long long dmg_split_extent64(SplitPlan plan) { return plan ? plan->impl->ext : -1; }
 

@@ -7,6 +7,8 @@
 size_t dmg_fft_pass_smem_f64(const dmg_fft_pass *p);
 size_t dmg_fft_pass_smem_f32(const dmg_fft_pass *p);
 size_t dmg_fft_pass_smem_df(const dmg_fft_pass *p);
+size_t dmg_fft_pass_smem_tc(const dmg_fft_pass *p);
+int dmg_fft_pass_launch_tc(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream);
 int dmg_fft_pass_launch_f64(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream);
 int dmg_fft_pass_launch_f32(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream);
 int dmg_fft_pass_launch_df(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream);
@@ -62,7 +64,9 @@ __global__ void __launch_bounds__(256) maxexp_rows_kernel(const dmg_fft_layout l
 }  // namespace
 
 extern "C" size_t dmg_fft_pass_smem(const dmg_fft_pass *p, int dtype) {
-  return dtype == 0 ? dmg_fft_pass_smem_f64(p) : dtype == 1 ? dmg_fft_pass_smem_f32(p) : dmg_fft_pass_smem_df(p);
+  return dtype == 0 ? dmg_fft_pass_smem_f64(p)
+                    : dtype == 1 ? dmg_fft_pass_smem_f32(p)
+                                 : dtype == 2 ? dmg_fft_pass_smem_df(p) : dmg_fft_pass_smem_tc(p);
 }
 
 extern "C" int dmg_fft_pass_launch_batch(const dmg_fft_pass *p, int dtype, const dmg_fft_batch *b, void *stream) {
@@ -74,6 +78,7 @@ extern "C" int dmg_fft_pass_launch_batch(const dmg_fft_pass *p, int dtype, const
     case 0: return dmg_fft_pass_launch_f64(p, b, stream);
     case 1: return dmg_fft_pass_launch_f32(p, b, stream);
     case 2: return dmg_fft_pass_launch_df(p, b, stream);
+    case 3: return dmg_fft_pass_launch_tc(p, b, stream);
     default: return dmg_error(DMG_ERR_ARG, "fft dtype %d", dtype);
   }
 }

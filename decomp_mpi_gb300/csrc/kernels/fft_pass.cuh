@@ -54,6 +54,7 @@
 #include <type_traits>
 #include "../host/dmg_internal.h"
 #include "../host/fft_params.h"
+#include "tc_sm100.cuh"
 
 namespace {
 
@@ -933,8 +934,19 @@ __host__ __device__ constexpr bool fixed_length(int n) {
          n == 48 || n == 96 || n == 120 || n == 160 || n == 192 || n == 240 || n == 320 || n == 384 || n == 480;
 }
 
+// The tensor-core form of the 1024-point FP32 pass (tc = true) keeps, after
+// the staging buffer, an area of TC_AREA bytes (aligned at run time to 1024
+// bytes inside it): the two A operands of a product (hi and lo halves, 16 KB
+// each; the line-padded result after the second product), the two B operands
+// (the 32-point DFT matrix's hi and lo halves, 8 KB each) and the rows' scale
+// exponents.
+constexpr size_t TC_A_BYTES = 33792;  // >= 32 KB of operands and >= 4 lines x 1025 x 8 bytes of result
+constexpr size_t TC_B_BYTES = 16384;
+constexpr size_t TC_EXP_BYTES = 1024;
+constexpr size_t TC_AREA = 1024 + TC_A_BYTES + TC_B_BYTES + TC_EXP_BYTES;
+
 template <typename T>
-__host__ __device__ inline SmemLayout smem_layout(const dmg_fft_pass &p, bool fixed) {
+__host__ __device__ inline SmemLayout smem_layout(const dmg_fft_pass &p, bool fixed, bool tc = false) {
   SmemLayout s;
   const size_t es = sizeof(C2<T>);
   const int n = p.n;
@@ -942,9 +954,9 @@ __host__ __device__ inline SmemLayout smem_layout(const dmg_fft_pass &p, bool fi
   const size_t one = fixed && pow2_length(n) ? pow2_stride(es, n) : (size_t)p.M1 * p.M2 * s.ld * es;
   s.buf_a = one;
   s.buf_b = 2 * one;
-  size_t pos = (3 * one + 15) & ~(size_t)15;
+  size_t pos = tc ? ((one + TC_AREA + 15) & ~(size_t)15) : ((3 * one + 15) & ~(size_t)15);
   s.roots_off = pos;
-  if (fixed && (pow2_length(n) ? !global_twiddles(n, es) : DMG_FFT_SMEM_ROOTS)) pos += (size_t)n * es;
+  if (!tc && fixed && (pow2_length(n) ? !global_twiddles(n, es) : DMG_FFT_SMEM_ROOTS)) pos += (size_t)n * es;
   s.contrib_off = pos;
   pos += (size_t)3 * parts_len(p) * sizeof(int64_t);
   s.spos_off = pos;
@@ -1088,6 +1100,10 @@ struct PassConsts {
   int64_t t0base_in, t0base_out;  // their first entries
   int ndig, rad[NDIG], inc[NDIG], dig[NDIG];
   TileState ts[3];  // the tile being transformed, the one being gathered, the one after
+  // tensor-core form: the MMA completion barrier, the tensor-memory columns, a wait that gave up
+  uint64_t tc_bar;
+  uint32_t tc_taddr;
+  int tc_fail;
 };
 
 __device__ __forceinline__ void tile_digits(const int *rad, int nd, int64_t t, int *dig) {
@@ -1413,9 +1429,204 @@ __device__ __forceinline__ void gather_async(const dmg_fft_pass &p, const PassCo
   copy_async_commit();
 }
 
+// ---------------------------------------------------------------- tensor-core stages (1024-point FP32 lines)
+//
+// The 1024-point DFT of a line as two 32-point DFT products on the tensor
+// cores (four-step: t = t1 + 32 t2, k = k2 + 32 k1):
+//   Z[t1, k2] = sum_t2 x[t1 + 32 t2] w32^(t2 k2)                 (product 1)
+//   X[k2 + 32 k1] = sum_t1 (Z[t1, k2] w1024^(t1 k2)) w32^(t1 k1)  (product 2)
+// A tile's four lines give M = 4 x 32 = 128 rows (row = line * 32 + t1, then
+// line * 32 + k2); a complex value is two real columns (re, im), so each
+// product is D[128 x 64] = A[128 x 64] B[64 x 64]^T with B the real form of
+// the 32-point DFT matrix ([c, -s; s, c] blocks).  Operands are split into
+// FP16 hi + lo parts and D = Al Bh + Ah Bl + Ah Bh accumulates in FP32 in
+// tensor memory; each row is scaled by a power of two first so that its
+// largest magnitude lies in [2^14, 2^15) (FP16's range), and the product is
+// scaled back as it leaves tensor memory.  The twiddle w1024^(t1 k2) is
+// applied in FP32 between the products.
+
+// MMA completion waits give up after this many polls (a fault, not a slow
+// product: one product takes well under a microsecond)
+constexpr uint32_t TC_WAIT_LIMIT = 1u << 22;
+
+// 2^e as a float, e in [-126, 126]
+__device__ __forceinline__ float tc_pow2(int e) { return __uint_as_float((uint32_t)(127 + e) << 23); }
+
+// scale exponent of a row whose largest |component| has the bit pattern m
+__device__ __forceinline__ int tc_row_exp(uint32_t m) {
+  if (m == 0) return 0;
+  const int e = (int)(m >> 23) - 127 - 14;
+  return e < -126 ? -126 : (e > 126 ? 126 : e);
+}
+
+__device__ __forceinline__ uint32_t tc_bits(__half2 h) {
+  uint32_t u;
+  memcpy(&u, &h, sizeof(u));
+  return u;
+}
+
+// v * 2^-e split into FP16 hi and lo pairs (re, im each)
+__device__ __forceinline__ void tc_split(float2 v, float sc, __half2 &hi, __half2 &lo) {
+  const float2 xs = pmul(v, splat(sc));
+  hi = __float22half2_rn(xs);
+  const float2 back = __half22float2(hi);
+  lo = __float22half2_rn(psub(xs, back));
+}
+
+// The real form of the 32-point DFT matrix (conjugated for the inverse) as
+// the B operand, hi and lo halves: row n = 2 k + a, column 2 t + b.
+// roots: the pass's 1024 roots exp(-2 pi i m / 1024).
+template <int SIGN>
+__device__ __forceinline__ void tc_build_dft32(const float2 *roots, unsigned char *Bm, int tid) {
+  for (int e = tid; e < 64 * 64; e += NT) {
+    const int n = e >> 6, kk = e & 63;
+    const int k = n >> 1, a = n & 1, t = kk >> 1, b = kk & 1;
+    float2 w = __ldg(roots + 32 * ((t * k) & 31));
+    if (SIGN > 0) w.y = -w.y;
+    const float val = a == 0 ? (b == 0 ? w.x : -w.y) : (b == 0 ? w.y : w.x);
+    const __half hi = __float2half_rn(val);
+    const __half lo = __float2half_rn(val - __half2float(hi));
+    *reinterpret_cast<__half *>(Bm + tc::sw128_offset(n, kk)) = hi;
+    *reinterpret_cast<__half *>(Bm + TC_B_BYTES / 2 + tc::sw128_offset(n, kk)) = lo;
+  }
+}
+
+// D = Al Bh + Ah Bl + Ah Bh over K = 64 (four slices of 16), then a commit
+// to the barrier; one thread issues it.  The small cross terms go first: the
+// accumulator rounds after every MMA, and this way only the last four
+// additions round at the full magnitude of the result.
+__device__ __forceinline__ void tc_issue(uint32_t taddr, uint32_t a_sa, uint32_t b_sa, uint32_t bar) {
+  constexpr uint32_t ID = tc::idesc_f16_f32(128, 64);
+  constexpr uint32_t LO_A = 16384, LO_B = (uint32_t)(TC_B_BYTES / 2);
+  static_assert(TC_A_BYTES >= 2 * LO_A, "two A operands");
+#pragma unroll
+  for (int kk = 0; kk < 4; ++kk)
+    tc::mma_f16(taddr, tc::desc_sw128(a_sa + LO_A + 32 * kk), tc::desc_sw128(b_sa + 32 * kk), ID, kk > 0);
+#pragma unroll
+  for (int kk = 0; kk < 4; ++kk)
+    tc::mma_f16(taddr, tc::desc_sw128(a_sa + 32 * kk), tc::desc_sw128(b_sa + LO_B + 32 * kk), ID, 1);
+#pragma unroll
+  for (int kk = 0; kk < 4; ++kk)
+    tc::mma_f16(taddr, tc::desc_sw128(a_sa + 32 * kk), tc::desc_sw128(b_sa + 32 * kk), ID, 1);
+  tc::mma_commit(bar);
+}
+
+// Product 1's operand from the staging buffer (line l, value t at
+// l * ld + swz(t)): thread pairs own rows (l, t1), each thread 16 of the 32
+// values x[t1 + 32 t2]; lines >= nlines are zero.  Ends with the operands
+// visible to the tensor cores and a barrier.
+__device__ __forceinline__ void tc_operand1(const float2 *stg, int ld, unsigned char *A, int *exp1, int nlines,
+                                            int tid) {
+  const int r = tid >> 1, h = tid & 1;
+  const int l = r >> 5, t1 = r & 31;
+  float2 x[16];
+  uint32_t mx = 0;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    x[i] = l < nlines ? stg[l * ld + swz<float, 1024>(t1 + 32 * (16 * h + i))] : make_float2(0.f, 0.f);
+    mx = max(mx, max(__float_as_uint(x[i].x) & 0x7FFFFFFFu, __float_as_uint(x[i].y) & 0x7FFFFFFFu));
+  }
+  mx = max(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, 1));
+  const int e = tc_row_exp(mx);
+  const float sc = tc_pow2(-e);
+  const uint32_t rowb = (uint32_t)(r >> 3) * 1024u + (uint32_t)(r & 7) * 128u;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    uint32_t hb[4], lb[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      __half2 hv, lv;
+      tc_split(x[4 * j + q], sc, hv, lv);
+      hb[q] = tc_bits(hv);
+      lb[q] = tc_bits(lv);
+    }
+    const uint32_t off = rowb + ((uint32_t)((4 * h + j) ^ (r & 7)) << 4);
+    *reinterpret_cast<uint4 *>(A + off) = make_uint4(hb[0], hb[1], hb[2], hb[3]);
+    *reinterpret_cast<uint4 *>(A + 16384 + off) = make_uint4(lb[0], lb[1], lb[2], lb[3]);
+  }
+  if (h == 0) exp1[r] = e;
+  tc::fence_proxy_async();
+  __syncthreads();
+}
+
+// Waits for product 1, applies the row scale and the twiddle, builds product
+// 2's operand (rows (l, k2), columns t1), waits for product 2 and writes the
+// lines, scaled back, in natural order (value k at l * ld + swz(k)) over the
+// A area.  Warp w reads tensor-memory lanes 32 (w % 4) .. + 31 (line w % 4,
+// t1 or k2 = lane) and the column half w / 4.  Ends with a barrier.
+template <int SIGN>
+__device__ __forceinline__ const float2 *tc_finish(unsigned char *A, uint32_t a_sa, uint32_t b_sa, int *exp1,
+                                                   int *exp2, const float2 *roots, int ld, uint32_t taddr,
+                                                   uint32_t bar, uint32_t &phase, int &fail, int tid) {
+  const int w = tid >> 5, lane = tid & 31, l = w & 3, hf = w >> 2;
+  const uint32_t lane_addr = taddr + ((uint32_t)(32 * l) << 16) + (uint32_t)(32 * hf);
+  bool ok = !fail && tc::mbar_wait(bar, phase & 1u, TC_WAIT_LIMIT);
+  ++phase;
+  tc::fence_after_sync();
+  float d[32];
+  if (ok) {
+    tc::tmem_ld16(lane_addr, d);
+    tc::tmem_ld16(lane_addr + 16, d + 16);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 32; ++i) d[i] = 0.f;
+  }
+  {
+    const float s1 = tc_pow2(exp1[32 * l + lane]);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      const int k2 = 16 * hf + j;
+      float2 wt = __ldg(roots + lane * k2);
+      if (SIGN > 0) wt.y = -wt.y;
+      const float2 z = cmul(pmul(make_float2(d[2 * j], d[2 * j + 1]), splat(s1)), wt);
+      uint32_t m = max(__float_as_uint(z.x) & 0x7FFFFFFFu, __float_as_uint(z.y) & 0x7FFFFFFFu);
+      m = __reduce_max_sync(0xFFFFFFFFu, m);
+      const int e2 = tc_row_exp(m);
+      __half2 hv, lv;
+      tc_split(z, tc_pow2(-e2), hv, lv);
+      const int r2 = 32 * l + k2;
+      const uint32_t off = (uint32_t)(r2 >> 3) * 1024u + (uint32_t)(r2 & 7) * 128u +
+                           ((uint32_t)((lane >> 2) ^ (r2 & 7)) << 4) + (uint32_t)(lane & 3) * 4u;
+      *reinterpret_cast<__half2 *>(A + off) = hv;
+      *reinterpret_cast<__half2 *>(A + 16384 + off) = lv;
+      if (lane == 0) exp2[r2] = e2;
+    }
+  }
+  tc::fence_proxy_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  if (tid == 0 && ok) {
+    tc::fence_after_sync();
+    tc_issue(taddr, a_sa, b_sa, bar);
+  }
+  ok = ok && tc::mbar_wait(bar, phase & 1u, TC_WAIT_LIMIT);
+  ++phase;
+  tc::fence_after_sync();
+  if (ok) {
+    tc::tmem_ld16(lane_addr, d);
+    tc::tmem_ld16(lane_addr + 16, d + 16);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 32; ++i) d[i] = 0.f;
+  }
+  float2 *res = reinterpret_cast<float2 *>(A);
+  const float s2 = tc_pow2(exp2[32 * l + lane]);
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const int k = lane + 32 * (16 * hf + j);
+    res[l * ld + swz<float, 1024>(k)] = pmul(make_float2(d[2 * j], d[2 * j + 1]), splat(s2));
+  }
+  if (!ok) fail = 1;
+  tc::fence_before_sync();
+  __syncthreads();
+  return res;
+}
+
 // NF > 0: length NF with a compile-time schedule; NF == 0: any length.
-template <typename T, int SIGN, int NF>
+// TC: the 1024-point FP32 pass with its DFT on the tensor cores (see above).
+template <typename T, int SIGN, int NF, bool TC = false>
 __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p, const dmg_fft_batch bt) {
+  static_assert(!TC || (std::is_same<T, float>::value && NF == 1024), "tensor-core stages: 1024-point FP32");
   constexpr bool FIXED = NF > 0;
   // power-of-two lengths: buffers at compile-time offsets (staging, A, B, twiddle tables)
   constexpr bool POW2 = pow2_length(NF);
@@ -1425,7 +1636,7 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
   const int tid = threadIdx.x;
   const int64_t ntiles_all = p.ntiles * bt.count;
   if (tid == 0) {
-    const SmemLayout S = smem_layout<T>(p, FIXED);
+    const SmemLayout S = smem_layout<T>(p, FIXED, TC);
     kc.ld = S.ld;
     kc.M1 = p.M1;
     kc.buf_a = (unsigned)S.buf_a;
@@ -1462,8 +1673,28 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
       digits_add(kc.dig, kc.inc, kc.rad, nd);
       if (blockIdx.x + gridDim.x < ntiles_all) tile_state_digits<T>(p, bt, kc.dig, kc.ts[1]);
     }
+    if constexpr (TC) {
+      kc.tc_fail = 0;
+      tc::mbar_init(tc::smem_u32(&kc.tc_bar), 1);
+    }
+  }
+  // tensor-core form: the area after the staging buffer, 1024-byte aligned; 64 tensor-memory columns (one
+  // 128 x 64 FP32 accumulator)
+  unsigned char *tcA = nullptr, *tcB = nullptr;
+  int *tcE1 = nullptr, *tcE2 = nullptr;
+  uint32_t tc_phase = 0;
+  if constexpr (TC) {
+    const uint32_t at = tc::smem_u32(sm) + (uint32_t)PSTRIDE;
+    tcA = sm + PSTRIDE + ((1024u - (at & 1023u)) & 1023u);
+    tcB = tcA + TC_A_BYTES;
+    tcE1 = reinterpret_cast<int *>(tcB + TC_B_BYTES);
+    tcE2 = tcE1 + 128;
+    if (tid < 32) tc::tmem_alloc(tc::smem_u32(&kc.tc_taddr), 64);
+    tc_build_dft32<SIGN>(reinterpret_cast<const float2 *>(p.roots), tcB, tid);
+    tc::fence_before_sync();
   }
   __syncthreads();
+  if constexpr (TC) tc::fence_after_sync();
   // separable address parts: gather side, two scatter-side areas (tiles alternate)
   int64_t *const parts_in = reinterpret_cast<int64_t *>(sm + kc.contrib_off);
   int64_t *const parts_out0 = parts_in + parts_len(p);
@@ -1576,7 +1807,14 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
       const int nlines = p.M1 * p.M2;
       const C2<T> *stg = reinterpret_cast<const C2<T> *>(sm);
       C2<T> *bufA = reinterpret_cast<C2<T> *>(sm + (POW2 ? PSTRIDE : kc.buf_a));
-      if constexpr (POW2) {
+      if constexpr (TC) {
+        (void)bufA;
+        tc_operand1(reinterpret_cast<const float2 *>(stg), ld, tcA, tcE1, nlines, tid);
+        if (tid == 0 && !kc.tc_fail) {
+          tc::fence_after_sync();
+          tc_issue(kc.tc_taddr, tc::smem_u32(tcA), tc::smem_u32(tcB), tc::smem_u32(&kc.tc_bar));
+        }
+      } else if constexpr (POW2) {
         stage_pow2<T, SIGN, NF, 1>(stg, bufA, reinterpret_cast<const C2<T> *>(sm + 3 * PSTRIDE), nlines, ld, tid,
                                    conv_first, kc.ts[cur].sexp);
       } else if constexpr (FIXED) {
@@ -1599,7 +1837,14 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
       const int nlines = p.M1 * p.M2;
       C2<T> *bufA = reinterpret_cast<C2<T> *>(sm + (POW2 ? PSTRIDE : kc.buf_a));
       C2<T> *bufB = reinterpret_cast<C2<T> *>(sm + (POW2 ? 2 * PSTRIDE : kc.buf_b));
-      if constexpr (FIXED) {
+      if constexpr (TC) {
+        (void)bufA;
+        (void)bufB;
+        res = reinterpret_cast<const C2<T> *>(tc_finish<SIGN>(tcA, tc::smem_u32(tcA), tc::smem_u32(tcB), tcE1, tcE2,
+                                                               reinterpret_cast<const float2 *>(p.roots), ld,
+                                                               kc.tc_taddr, tc::smem_u32(&kc.tc_bar), tc_phase,
+                                                               kc.tc_fail, tid));
+      } else if constexpr (FIXED) {
         const C2<T> *rts = POW2 ? (global_twiddles(NF, sizeof(C2<T>)) ? reinterpret_cast<const C2<T> *>(p.roots)
                                                                       : reinterpret_cast<const C2<T> *>(sm + 3 * PSTRIDE))
                            : DMG_FFT_SMEM_ROOTS ? reinterpret_cast<const C2<T> *>(sm + kc.roots_off)
@@ -1695,12 +1940,18 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
     }
     __syncthreads();
   }
+  if constexpr (TC) {
+    // every tensor-memory read is done (each tile ends with a barrier): give the columns back
+    tc::fence_after_sync();
+    if (tid < 32) tc::tmem_dealloc(kc.tc_taddr, 64);
+    if (tid == 0 && kc.tc_fail && p.status) atomicExch(p.status, 1);
+  }
 }
 
-template <typename T, int SIGN, int NF>
+template <typename T, int SIGN, int NF, bool TC = false>
 int launch_k(const dmg_fft_pass &p, const dmg_fft_batch &bt, cudaStream_t s) {
-  const size_t smem = smem_layout<T>(p, NF > 0).total;
-  auto k = fft_pass_kernel<T, SIGN, NF>;
+  const size_t smem = smem_layout<T>(p, NF > 0, TC).total;
+  auto k = fft_pass_kernel<T, SIGN, NF, TC>;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return dmg_error(DMG_ERR_CUDA, "fft pass smem %zu: %s", smem, cudaGetErrorString(e));

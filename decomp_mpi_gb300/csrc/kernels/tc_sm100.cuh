@@ -1,0 +1,125 @@
+// Blackwell (sm_100 family) tensor-core building blocks in inline PTX:
+// tensor-memory allocation, shared-memory matrix descriptors, the
+// instruction descriptor of a kind::f16 MMA, the MMA itself with its commit
+// to an mbarrier, bounded mbarrier waits, and loads from tensor memory.
+//
+// Conventions used by the FFT passes:
+//  * operands are K-major with the 128-byte swizzle: a matrix of R rows and
+//    64 half-precision columns (128 bytes per row) is stored as R/8 atoms of
+//    8 rows x 128 bytes, atom after atom (stride 1024 bytes); inside an atom
+//    row r's 16-byte chunk c sits at chunk position c ^ (r % 8).  The atom
+//    base must be 1024-byte aligned.
+//  * one MMA consumes K = 16 columns (32 bytes of a row): the k-th slice is
+//    addressed by advancing the descriptor's start address by 32 * k bytes.
+//  * the accumulator is FP32 in tensor memory: row m of an M = 128 tile is
+//    TMEM lane m, column n is TMEM column (base + n).
+#pragma once
+#include <cuda_fp16.h>
+#include <cstdint>
+
+namespace tc {
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// byte offset of element (r, k) (half precision) in a K-major, 128-byte
+// swizzled operand of 64 columns
+__host__ __device__ constexpr uint32_t sw128_offset(uint32_t r, uint32_t k) {
+  return (r >> 3) * 1024u + (r & 7u) * 128u + ((((k * 2u) >> 4) ^ (r & 7u)) << 4) + ((k * 2u) & 15u);
+}
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms
+// 1024 bytes apart (stride byte offset), start address `saddr` (16-byte
+// units in bits 0-13), descriptor version 1 (bits 46-47), swizzle mode 2
+// (bits 61-63)
+__device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;                  // leading byte offset (unused by swizzled K-major operands)
+  d |= (uint64_t)(1024u >> 4) << 32;       // stride byte offset: 8-row atoms
+  d |= (uint64_t)1 << 46;                  // version
+  d |= (uint64_t)2 << 61;                  // 128-byte swizzle
+  return d;
+}
+
+// instruction descriptor of kind::f16: D in FP32, A and B in FP16, both
+// K-major, M x N
+__host__ __device__ constexpr uint32_t idesc_f16_f32(int M, int N) {
+  return (1u << 4)                            // D format: F32
+         | (0u << 7) | (0u << 10)             // A, B format: F16
+         | (0u << 15) | (0u << 16)            // A, B K-major
+         | ((uint32_t)(N >> 3) << 17)         // N / 8
+         | ((uint32_t)(M >> 4) << 24);        // M / 16
+}
+
+// ---- tensor memory ----
+// allocate `ncols` columns (a power of two >= 32) for this CTA; one whole warp
+// executes it; the address lands in shared memory at `dst`
+__device__ __forceinline__ void tmem_alloc(uint32_t dst_saddr, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(dst_saddr), "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+// generic-proxy writes to shared memory become visible to the tensor cores
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
+// ---- mbarriers ----
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+// wait for the phase with parity `parity` to complete; gives up after
+// `limit` polls (each poll may suspend the thread for a while) and returns
+// false then
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint32_t limit) {
+  for (uint32_t i = 0; i < limit; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// ---- MMA ----
+// D[tmem] (+)= A[smem] * B[smem]^T for one K = 16 slice; accum = 0 overwrites D
+__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                        uint32_t accum) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum)
+      : "memory");
+}
+// arrive on the mbarrier once every MMA this thread issued before has completed
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
+               : "memory");
+}
+
+// ---- tensor memory -> registers ----
+// 32 lanes x 32 bits, 16 consecutive columns: thread i of the warp gets lane
+// (lane base + i), columns col .. col + 15.  The wait for the load is part of
+// the same statement, so no use of the registers can be scheduled before it.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];\n"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+}  // namespace tc

@@ -138,13 +138,23 @@ SplitPlan dmg_makeParallelPlanTyped(Decomp start, int *initial_factor, void *dat
  * significand, relative error around 1e-14 on a 512^3 transform), computed
  * on the FP32 pipes; the input is scaled by a power of two so any FP64
  * magnitude fits.  DMG_ARITH_FP64 computes in native FP64 instead (GB300's
- * FP64 rate is about 1/56 of its FP32 rate).  complex64 plans use FP32. */
+ * FP64 rate is about 1/56 of its FP32 rate).  complex64 plans use FP32 by
+ * default; DMG_ARITH_TC16 runs the DFTs of their 1024-point passes as two
+ * 32-point DFT products on the tensor cores (FP16 hi + lo operands, three
+ * products each, FP32 accumulation, a power-of-two scale per row; other
+ * lengths keep the FP32 stages). */
 #define DMG_ARITH_FP64 0
 #define DMG_ARITH_FP32 1
 #define DMG_ARITH_DF 2
+#define DMG_ARITH_TC16 3
 /** Select the arithmetic of a plan (DMG_ARITH_FP64 or DMG_ARITH_DF for
- * complex128; complex64 plans accept only DMG_ARITH_FP32). */
+ * complex128; DMG_ARITH_FP32 or DMG_ARITH_TC16 for complex64). */
 int dmg_split_set_arith(SplitPlan plan, int arith);
+/** The plan's device status word, read back after the work queued so far
+ * (a synchronising copy): 0 when every tensor-core pass completed its
+ * products, 1 when one gave up waiting for them (its results are wrong);
+ * negative on error. */
+int dmg_split_device_status(SplitPlan plan);
 /** The arithmetic a plan computes in (DMG_ARITH_*). */
 int dmg_split_get_arith(SplitPlan plan);
 /* Pass schedule.  Both give the reference's output in the same workspace

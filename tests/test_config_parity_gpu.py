@@ -12,7 +12,7 @@
   global-index pattern bit for bit, and the reverse reshape restores the
   source.
 * 1024^3 complex64 (complex Gaussian, 16 planted plane waves): the FP32
-  transform against the FP64 oracle on whole planes of the spectrum
+  and the tensor-core transforms against the FP64 oracle on whole planes of the spectrum
   (relative L2 and max-abs within 1e-6), Parseval's identity and the
   planted peaks.
 """
@@ -186,7 +186,7 @@ def _plane_oracle(x_host, n, k0s):
     return np.stack([O.fftn64(acc[i].reshape(n, n)) for i in range(len(k0s))])
 
 
-@pytest.mark.parametrize("arith", [api.ARITH_FP32], ids=["fp32"])
+@pytest.mark.parametrize("arith", [api.ARITH_FP32, api.ARITH_TC16], ids=["fp32", "tensor-core"])
 def test_c4_precision_1024_cubed(arith, cuda):
     import torch
     n, g = 1024, 8
@@ -210,6 +210,7 @@ def test_c4_precision_1024_cubed(arith, cuda):
     sp = api.SplitPlan(D, x.data_ptr(), wl, work.data_ptr(), dtype=api.C64)
     sp.set_arith(arith)
     sp.run(api.FFTW_FORWARD, st)
+    assert sp.device_status() == 0
     A, Bf, _, _, _, b_spec = O.split_factors(P, spec)
     assert sp.decomp_B().extent() == ext  # the gather below reads rank r's slots at r * ext
     # the spectrum in global frequency order on the device
@@ -238,9 +239,10 @@ def test_c4_precision_1024_cubed(arith, cuda):
     peak = float(np.abs(want).max())
     assert rel < 1e-6, rel
     assert max_abs / peak < 1e-6, max_abs / peak
-    # Parseval over the whole spectrum, and the planted waves at N (plus the noise's own coefficient)
+    # Parseval over the whole spectrum (an amplitude error of 1e-6 moves the energy by up to 2e-6), and the
+    # planted waves at N (plus the noise's own coefficient)
     spec_energy = float(torch.sum(out.abs().to(torch.float64) ** 2).item())
-    assert abs(spec_energy / N - energy) / energy < 1e-6
+    assert abs(spec_energy / N - energy) / energy < 2e-6
     for kv in waves:
         s = [int(inv[d][int(kv[d])]) for d in range(3)]
         v = complex(o3[s[0], s[1], s[2]].item())
