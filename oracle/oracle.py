@@ -85,6 +85,9 @@ def ref_lib():
         _sig(lib, "ref_reshape", ctypes.c_int,
              [ctypes.c_int, _cp, _cp, ctypes.c_int, _c_ll, _c_ll, _vp, _vp, _c_int_p, _c_int_p, _cp, ctypes.c_int])
         _sig(lib, "ref_processor_grid", ctypes.c_int, [ctypes.c_int, ctypes.c_int, _c_int_p, _c_int_p])
+        _sig(lib, "ref_time_step", ctypes.c_int,
+             [ctypes.c_int, _cp, _cp, _cp, _c_ll, _c_ll, _c_ll, _c_ll, _vp, _vp, _vp, _vp, ctypes.c_int,
+              ctypes.c_int, ctypes.POINTER(ctypes.c_double), _cp, ctypes.c_int])
         _sig(lib, "ref_split", ctypes.c_int,
              [ctypes.c_int, _cp, ctypes.c_int, _c_int_p, _c_ll, _c_ll, _vp, _vp, _c_int_p, _c_ll_p, ctypes.c_int,
               _cp, ctypes.c_int])
@@ -247,6 +250,20 @@ def ref_split(P, start_spec, dat: np.ndarray, dat_pitch, work_len, mode=0, B=Non
         raise RuntimeError("reference split failed: %s" % err.value.decode())
     info = np.array(list(info), dtype=np.int64).reshape(P, 8)
     return work, info, slot
+
+
+def ref_time_step(P, specs, pitches, work_len, arrays, warmup, steps):
+    """Wall seconds of `steps` benchmark steps (two reshapes, split FFT forward and backward) run by the
+    reference's own code on P thread-ranks, after `warmup` steps."""
+    err = ctypes.create_string_buffer(512)
+    sec = ctypes.c_double()
+    a0, a1, a2, work = arrays
+    rc = ref_lib().ref_time_step(P, specs[0].encode(), specs[1].encode(), specs[2].encode(), pitches[0], pitches[1],
+                                 pitches[2], work_len, a0.ctypes.data, a1.ctypes.data, a2.ctypes.data,
+                                 work.ctypes.data, warmup, steps, ctypes.byref(sec), err, 512)
+    if rc:
+        raise RuntimeError("reference step failed: %s" % err.value.decode())
+    return sec.value
 
 
 # ---------------------------------------------------------------- FFT value oracle

@@ -202,3 +202,67 @@ int ref_split(int P, const char *start_spec, int mode, const int *B, long long d
   if (rc && err) snprintf(err, errlen, "%s", shim_error());
   return rc;
 }
+
+/* ---- timing of the benchmark step (calibration of the CPU port against the reference itself) ---- */
+
+#include <time.h>
+
+typedef struct {
+  const char *s0, *s1, *s2; /* block, rotate, factor_reverse */
+  long long p0, p1, p2, work_len;
+  double *a0, *a1, *a2, *work;
+  int warmup, steps;
+  double seconds; /* rank 0: wall time of the timed steps */
+} step_job;
+
+static double now_s(void) {
+  struct timespec t;
+  clock_gettime(CLOCK_MONOTONIC, &t);
+  return t.tv_sec + 1e-9 * t.tv_nsec;
+}
+
+static void step_rank(int r, void *arg) {
+  step_job *j = (step_job *)arg;
+  Decomp d0 = build_decomp(j->s0), d1 = build_decomp(j->s1), d2 = build_decomp(j->s2);
+  MPI_Datatype base;
+  MPI_Type_contiguous(16, MPI_CHAR, &base);
+  MPI_Type_commit(&base);
+  ReshapePlan r01 = makeReshapePlan(MPI_COMM_WORLD, base, d0, d1);
+  ReshapePlan r12 = makeReshapePlan(MPI_COMM_WORLD, base, d1, d2);
+  double *a0 = j->a0 + 2 * (size_t)r * j->p0, *a1 = j->a1 + 2 * (size_t)r * j->p1;
+  fftw_complex *a2 = (fftw_complex *)(j->a2 + 2 * (size_t)r * j->p2);
+  fftw_complex *work = (fftw_complex *)(j->work + 2 * (size_t)r * j->work_len);
+  SplitPlan plan = makeSplitPlan(0, d2, a2, (int)j->work_len, work);
+  double t0 = 0;
+  for (int s = 0; s < j->warmup + j->steps; ++s) {
+    if (s == j->warmup) {
+      MPI_Barrier(MPI_COMM_WORLD);
+      t0 = now_s();
+    }
+    runReshapePlan(MPI_COMM_WORLD, r01, a0, a1);
+    runReshapePlan(MPI_COMM_WORLD, r12, a1, a2);
+    if (plan) {
+      runSplitPlan(plan, FFTW_FORWARD);
+      runSplitPlan(plan, FFTW_BACKWARD);
+    }
+  }
+  MPI_Barrier(MPI_COMM_WORLD);
+  if (r == 0) j->seconds = now_s() - t0;
+  freeReshapePlan(r01);
+  freeReshapePlan(r12);
+  MPI_Type_free(&base);
+}
+
+/* The benchmark step (two reshapes, the split FFT forward and backward) with
+ * the reference's own code on P thread-ranks: `steps` timed steps after
+ * `warmup`; returns their wall time in *seconds.  The arrays are whole
+ * virtual-grid arrays (rank r at r * pitch complex values). */
+int ref_time_step(int P, const char *s0, const char *s1, const char *s2, long long p0, long long p1, long long p2,
+                  long long work_len, double *a0, double *a1, double *a2, double *work, int warmup, int steps,
+                  double *seconds, char *err, int errlen) {
+  step_job j = {s0, s1, s2, p0, p1, p2, work_len, a0, a1, a2, work, warmup, steps, 0.0};
+  int rc = shim_run(P, step_rank, &j);
+  if (rc && err) snprintf(err, errlen, "%s", shim_error());
+  *seconds = j.seconds;
+  return rc;
+}
