@@ -88,6 +88,14 @@ SIGNATURES = {
     "proposeParallelPlan": (_vp, [_i, _vp, _ip, _vp, _i, _vp]),
     "buildParallelPlan": (_vp, [_i, _i, _i, _vp, _i, _ip, _ip, _ip, _ip, _ip, _vp, _i, _vp]),
     "autotuneParallelPlan": (_vp, [_vp, _vp, _i, _vp]),
+    "dmg_autotuneParallelPlanTyped": (_vp, [_vp, _vp, _ll, _vp, _i, _i]),
+    "dmg_autotune_cache_clear": (None, []),
+    "dmg_autotune_cache_entries": (_i, []),
+    "dmg_autotune_last_timed": (_i, []),
+    "dmg_split_set_tile": (_i, [_vp, _i]),
+    "dmg_split_get_tile": (_i, [_vp]),
+    "dmg_split_set_radix": (_i, [_vp, _i]),
+    "dmg_split_get_radix": (_i, [_vp]),
     "dmg_makeSplitPlanTyped": (_vp, [_i, _vp, _vp, _ll, _vp, _i]),
     "dmg_makeParallelPlanTyped": (_vp, [_vp, _ip, _vp, _ll, _vp, _i]),
     "runSplitPlan": (None, [_vp, _i]),

@@ -32,6 +32,9 @@ ARITH_TC16 = 3
 SCHEDULE_AUTO = 0
 SCHEDULE_LINES = 1
 SCHEDULE_SPLIT = 2
+RADIX_FIXED = 0
+RADIX_PLAN8 = 1
+RADIX_PLAN4 = 2
 # SearchFlags of split_fft.h
 NO_FLAGS = 0x00
 PREFER_LARGE_FFT = 0x01
@@ -357,13 +360,14 @@ class SplitPlan:
     """
 
     def __init__(self, start: Decomp, dat_ptr: int, length: int, work_ptr: int, slab: int = 0, B=None,
-                 dtype: int = C128, autotune: bool = False, arith=None, schedule=None):
+                 dtype: int = C128, autotune: bool = False, arith=None, schedule=None, full_grid: bool = False):
         self.lib = load()
         self.start = start
-        if autotune:
-            if dtype != C128:
-                raise ValueError("autotuneParallelPlan is complex128")
+        if autotune and dtype == C128 and not full_grid:
             h = self.lib.autotuneParallelPlan(start.h, ctypes.c_void_p(dat_ptr), int(length), ctypes.c_void_p(work_ptr))
+        elif autotune:
+            h = self.lib.dmg_autotuneParallelPlanTyped(start.h, ctypes.c_void_p(dat_ptr), int(length),
+                                                       ctypes.c_void_p(work_ptr), int(dtype), int(bool(full_grid)))
         elif B is not None:
             h = self.lib.dmg_makeParallelPlanTyped(start.h, _int_array(B), ctypes.c_void_p(dat_ptr), int(length),
                                                    ctypes.c_void_p(work_ptr), int(dtype))
@@ -417,6 +421,22 @@ class SplitPlan:
     @property
     def schedule(self):
         return self.lib.dmg_split_get_schedule(self.h)
+
+    def set_tile(self, values):
+        """Values per pass tile (0: the default)."""
+        check(self.lib.dmg_split_set_tile(self.h, int(values)), "dmg_split_set_tile")
+
+    @property
+    def tile(self):
+        return self.lib.dmg_split_get_tile(self.h)
+
+    def set_radix(self, radix):
+        """RADIX_FIXED (compile-time radix schedules), RADIX_PLAN8 or RADIX_PLAN4 (the plan's radices)."""
+        check(self.lib.dmg_split_set_radix(self.h, int(radix)), "dmg_split_set_radix")
+
+    @property
+    def radix(self):
+        return self.lib.dmg_split_get_radix(self.h)
 
     @property
     def _s(self):
@@ -496,6 +516,20 @@ class SplitPlan:
             self.free()
         except Exception:
             pass
+
+
+def autotune_cache_clear():
+    """Forget every cached autotuning winner."""
+    load().dmg_autotune_cache_clear()
+
+
+def autotune_cache_entries() -> int:
+    return load().dmg_autotune_cache_entries()
+
+
+def autotune_last_timed() -> int:
+    """Configurations the last autotuning call timed (0 when it built a cached choice)."""
+    return load().dmg_autotune_last_timed()
 
 
 def _wrap_plan(start: Decomp, handle, length: int) -> "SplitPlan":

@@ -55,6 +55,8 @@ struct dmg_fft_pass {
   int32_t load_pos[3], store_pos[3];
   int32_t nfac;
   int32_t fac[DMG_FFT_MAXFAC]; /* radices, first stage first */
+  int32_t radix_runtime;       /* run the radices above in the runtime-length kernel even where the length has
+                                  a compile-time schedule */
   const void *roots;           /* n roots exp(-2 pi i k / n), double2 or float2 */
   int32_t sign;                /* -1 forward, +1 inverse */
   /* split twiddle of the transformed dimension d = t/2 (t a z sub-axis):

@@ -72,6 +72,8 @@ struct dmg_split_impl {
   int grid_a[DMG_FFT_MAXDIM], grid_b[DMG_FFT_MAXDIM];
   int use_first, use_second;
   int schedule;        /* DMG_SCHEDULE_*: as asked */
+  int tile_values;     /* values per pass tile (0: the default for the element size) */
+  int radix;           /* DMG_RADIX_*: the passes' radix schedules */
   int lines;           /* the passes built are the lines schedule */
   long long length;    /* per-rank workspace length */
   long long ext;       /* largest extent of A and B */
@@ -216,14 +218,16 @@ static int64_t sub_step(const struct dmg_split_impl *im, const fft_layout *l, co
   return st < 0 ? -st : st;
 }
 
-/* radices of n: 8s, then 4, 2, 3, 5, then other primes */
-static int factorize(int n, int32_t *fac) {
+/* radices of n: 8s, then 4, 2, 3, 5, then other primes (fours: 4s, then 2,
+ * 3, 5, other primes) */
+static int factorize(int n, int32_t *fac, int fours) {
   int k = 0;
-  while (n % 8 == 0) {
+  while (!fours && n % 8 == 0) {
     fac[k++] = 8;
     n /= 8;
   }
-  if (n % 4 == 0) {
+  while (n % 4 == 0) {
+    if (k >= DMG_FFT_MAXFAC) return -1;
     fac[k++] = 4;
     n /= 4;
   }
@@ -280,7 +284,8 @@ static int pass_geometry(const struct dmg_split_impl *im, struct dmg_fft_pass *p
   p->t = t;
   p->n = sub_len(A, B, t);
   if (p->n > 4096) return dmg_error(DMG_ERR_UNSUPPORTED, "FFT factor %d exceeds 4096", p->n);
-  p->nfac = factorize(p->n, p->fac);
+  p->nfac = factorize(p->n, p->fac, im->radix == DMG_RADIX_PLAN4);
+  p->radix_runtime = im->radix != DMG_RADIX_FIXED;
   if (p->nfac < 0) return dmg_error(DMG_ERR_UNSUPPORTED, "FFT length %d has too many prime factors", p->n);
   /* vector sub-axes: the most contiguous in either layout */
   int64_t best[2] = {INT64_MAX, INT64_MAX};
@@ -303,7 +308,7 @@ static int pass_geometry(const struct dmg_split_impl *im, struct dmg_fft_pass *p
   p->v2 = pick[1];
   p->nv1 = p->v1 >= 0 ? sub_len(A, B, p->v1) : 1;
   p->nv2 = p->v2 >= 0 ? sub_len(A, B, p->v2) : 1;
-  int room = DMG_FFT_TILE_TARGET(im->esize) / p->n;
+  int room = (im->tile_values > 0 ? im->tile_values : DMG_FFT_TILE_TARGET(im->esize)) / p->n;
   if (room < 1) room = 1;
   p->M1 = p->nv1 < room ? p->nv1 : room;
   room /= p->M1;
@@ -1091,6 +1096,45 @@ int dmg_split_set_schedule(SplitPlan plan, int schedule) {
 }
 
 int dmg_split_get_schedule(SplitPlan plan) { return plan ? (plan->impl->lines ? DMG_SCHEDULE_LINES : DMG_SCHEDULE_SPLIT) : -1; }
+
+/* rebuild the passes after a change of one of the plan's choices; on failure
+ * the old value is put back */
+static int rebuild_with(struct dmg_split_impl *im, int *field, int value) {
+  const int old = *field;
+  *field = value;
+  int st = build_passes(im);
+  if (st != DMG_OK) {
+    *field = old;
+    build_passes(im);
+    return st;
+  }
+  impl_free_device(im); /* passes point into the device tables: upload again */
+  return DMG_OK;
+}
+
+int dmg_split_set_tile(SplitPlan plan, int values) {
+  if (!plan) return dmg_error(DMG_ERR_ARG, "dmg_split_set_tile: NULL plan");
+  struct dmg_split_impl *im = plan->impl;
+  const int most = DMG_FFT_TILE_TARGET(im->esize);
+  if (values != 0 && (values < 64 || values > most || (values & (values - 1))))
+    return dmg_error(DMG_ERR_ARG, "dmg_split_set_tile: %d values per tile (0, or a power of two from 64 to %d)",
+                     values, most);
+  return rebuild_with(im, &im->tile_values, values);
+}
+
+int dmg_split_get_tile(SplitPlan plan) {
+  if (!plan) return -1;
+  return plan->impl->tile_values > 0 ? plan->impl->tile_values : DMG_FFT_TILE_TARGET(plan->impl->esize);
+}
+
+int dmg_split_set_radix(SplitPlan plan, int radix) {
+  if (!plan) return dmg_error(DMG_ERR_ARG, "dmg_split_set_radix: NULL plan");
+  if (radix != DMG_RADIX_FIXED && radix != DMG_RADIX_PLAN8 && radix != DMG_RADIX_PLAN4)
+    return dmg_error(DMG_ERR_ARG, "dmg_split_set_radix: radix schedule %d", radix);
+  return rebuild_with(plan->impl, &plan->impl->radix, radix);
+}
+
+int dmg_split_get_radix(SplitPlan plan) { return plan ? plan->impl->radix : -1; }
 
 int dmg_split_launches(SplitPlan plan, int direction) {
   if (!plan) return 0;

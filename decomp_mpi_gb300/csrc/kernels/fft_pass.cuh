@@ -975,7 +975,7 @@ __host__ __device__ inline SmemLayout smem_layout(const dmg_fft_pass &p, bool fi
 
 template <typename T>
 __host__ __device__ inline bool use_fixed(const dmg_fft_pass &p) {
-  return fixed_length(p.n);
+  return fixed_length(p.n) && !p.radix_runtime;
 }
 
 
@@ -1553,11 +1553,15 @@ __device__ __forceinline__ void tc_operand1(const float2 *stg, int ld, unsigned 
 // 2's operand (rows (l, k2), columns t1), waits for product 2 and writes the
 // lines, scaled back, in natural order (value k at l * ld + swz(k)) over the
 // A area.  Warp w reads tensor-memory lanes 32 (w % 4) .. + 31 (line w % 4,
-// t1 or k2 = lane) and the column half w / 4.  Ends with a barrier.
+// t1 or k2 = lane) and the column half w / 4.  Product 2's operand has one
+// scale per line: |Z[t1, k2]| <= 32 max_t2 |x[t1 + 32 t2]| < 2^(20 + e1[t1]),
+// so the exponent e2 = max_t1 e1[t1] + 5 keeps every value of the line below
+// 2^15 (and a power-of-two scale leaves the hi + lo split's relative
+// accuracy as it is).  Ends with a barrier.
 template <int SIGN>
-__device__ __forceinline__ const float2 *tc_finish(unsigned char *A, uint32_t a_sa, uint32_t b_sa, int *exp1,
-                                                   int *exp2, const float2 *roots, int ld, uint32_t taddr,
-                                                   uint32_t bar, uint32_t &phase, int &fail, int tid) {
+__device__ __forceinline__ const float2 *tc_finish(unsigned char *A, uint32_t a_sa, uint32_t b_sa, const int *exp1,
+                                                   const float2 *roots, int ld, uint32_t taddr, uint32_t bar,
+                                                   uint32_t &phase, int &fail, int tid) {
   const int w = tid >> 5, lane = tid & 31, l = w & 3, hf = w >> 2;
   const uint32_t lane_addr = taddr + ((uint32_t)(32 * l) << 16) + (uint32_t)(32 * hf);
   bool ok = !fail && tc::mbar_wait(bar, phase & 1u, TC_WAIT_LIMIT);
@@ -1565,31 +1569,30 @@ __device__ __forceinline__ const float2 *tc_finish(unsigned char *A, uint32_t a_
   tc::fence_after_sync();
   float d[32];
   if (ok) {
-    tc::tmem_ld16(lane_addr, d);
-    tc::tmem_ld16(lane_addr + 16, d + 16);
+    tc::tmem_ld32(lane_addr, d);
   } else {
 #pragma unroll
     for (int i = 0; i < 32; ++i) d[i] = 0.f;
   }
+  const int e1 = exp1[32 * l + lane];
+  const int e2 = min(__reduce_max_sync(0xFFFFFFFFu, e1) + 5, 126);
   {
-    const float s1 = tc_pow2(exp1[32 * l + lane]);
+    // back to the line's values (2^e1), then into product 2's range (2^-e2): two exact scalings, since
+    // 2^(e1 - e2) alone may lie below FP32's normal range
+    const float s1 = tc_pow2(e1), s2i = tc_pow2(-e2);
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
       const int k2 = 16 * hf + j;
       float2 wt = __ldg(roots + lane * k2);
       if (SIGN > 0) wt.y = -wt.y;
-      const float2 z = cmul(pmul(make_float2(d[2 * j], d[2 * j + 1]), splat(s1)), wt);
-      uint32_t m = max(__float_as_uint(z.x) & 0x7FFFFFFFu, __float_as_uint(z.y) & 0x7FFFFFFFu);
-      m = __reduce_max_sync(0xFFFFFFFFu, m);
-      const int e2 = tc_row_exp(m);
-      __half2 hv, lv;
-      tc_split(z, tc_pow2(-e2), hv, lv);
+      const float2 z = cmul(pmul(pmul(make_float2(d[2 * j], d[2 * j + 1]), splat(s1)), splat(s2i)), wt);
+      const __half2 hv = __float22half2_rn(z);
+      const __half2 lv = __float22half2_rn(psub(z, __half22float2(hv)));
       const int r2 = 32 * l + k2;
       const uint32_t off = (uint32_t)(r2 >> 3) * 1024u + (uint32_t)(r2 & 7) * 128u +
                            ((uint32_t)((lane >> 2) ^ (r2 & 7)) << 4) + (uint32_t)(lane & 3) * 4u;
       *reinterpret_cast<__half2 *>(A + off) = hv;
       *reinterpret_cast<__half2 *>(A + 16384 + off) = lv;
-      if (lane == 0) exp2[r2] = e2;
     }
   }
   tc::fence_proxy_async();
@@ -1603,14 +1606,13 @@ __device__ __forceinline__ const float2 *tc_finish(unsigned char *A, uint32_t a_
   ++phase;
   tc::fence_after_sync();
   if (ok) {
-    tc::tmem_ld16(lane_addr, d);
-    tc::tmem_ld16(lane_addr + 16, d + 16);
+    tc::tmem_ld32(lane_addr, d);
   } else {
 #pragma unroll
     for (int i = 0; i < 32; ++i) d[i] = 0.f;
   }
   float2 *res = reinterpret_cast<float2 *>(A);
-  const float s2 = tc_pow2(exp2[32 * l + lane]);
+  const float s2 = tc_pow2(e2);
 #pragma unroll
   for (int j = 0; j < 16; ++j) {
     const int k = lane + 32 * (16 * hf + j);
@@ -1681,14 +1683,13 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
   // tensor-core form: the area after the staging buffer, 1024-byte aligned; 64 tensor-memory columns (one
   // 128 x 64 FP32 accumulator)
   unsigned char *tcA = nullptr, *tcB = nullptr;
-  int *tcE1 = nullptr, *tcE2 = nullptr;
+  int *tcE1 = nullptr;
   uint32_t tc_phase = 0;
   if constexpr (TC) {
     const uint32_t at = tc::smem_u32(sm) + (uint32_t)PSTRIDE;
     tcA = sm + PSTRIDE + ((1024u - (at & 1023u)) & 1023u);
     tcB = tcA + TC_A_BYTES;
     tcE1 = reinterpret_cast<int *>(tcB + TC_B_BYTES);
-    tcE2 = tcE1 + 128;
     if (tid < 32) tc::tmem_alloc(tc::smem_u32(&kc.tc_taddr), 64);
     tc_build_dft32<SIGN>(reinterpret_cast<const float2 *>(p.roots), tcB, tid);
     tc::fence_before_sync();
@@ -1840,7 +1841,7 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
       if constexpr (TC) {
         (void)bufA;
         (void)bufB;
-        res = reinterpret_cast<const C2<T> *>(tc_finish<SIGN>(tcA, tc::smem_u32(tcA), tc::smem_u32(tcB), tcE1, tcE2,
+        res = reinterpret_cast<const C2<T> *>(tc_finish<SIGN>(tcA, tc::smem_u32(tcA), tc::smem_u32(tcB), tcE1,
                                                                reinterpret_cast<const float2 *>(p.roots), ld,
                                                                kc.tc_taddr, tc::smem_u32(&kc.tc_bar), tc_phase,
                                                                kc.tc_fail, tid));
@@ -1961,6 +1962,20 @@ int launch_k(const dmg_fft_pass &p, const dmg_fft_batch &bt, cudaStream_t s) {
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, NT, smem);
   if (per_sm < 1) return dmg_error(DMG_ERR_UNSUPPORTED, "fft pass does not fit on an SM (smem %zu)", smem);
+  if constexpr (TC) {
+    // the occupancy query answers one block per SM for kernels that allocate tensor memory; two blocks of
+    // this kernel fit (64 of the SM's 512 tensor-memory columns each, and shared memory and registers for
+    // two), and run together
+    cudaFuncAttributes fa;
+    int smem_sm = 0, reserve = 0;
+    if (cudaFuncGetAttributes(&fa, k) == cudaSuccess &&
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&reserve, cudaDevAttrReservedSharedMemoryPerBlock, dev) == cudaSuccess) {
+      const size_t per_block = smem + fa.sharedSizeBytes + (size_t)reserve;
+      const int fit = (int)((size_t)smem_sm / per_block);
+      per_sm = max(per_sm, min(fit, MINB));
+    }
+  }
   int64_t grid = (int64_t)nsm * per_sm;
   if (grid > p.ntiles * bt.count) grid = p.ntiles * bt.count;
   if (grid < 1) return DMG_OK;
@@ -1996,6 +2011,7 @@ int launch_pow2_group(const dmg_fft_pass &p, const dmg_fft_batch &bt, void *stre
 template <typename T, int SIGN>
 int launch_other_group(const dmg_fft_pass &p, const dmg_fft_batch &bt, void *stream) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (p.radix_runtime) return launch_k<T, SIGN, 0>(p, bt, s);
   switch (p.n) {
     case 48: return launch_k<T, SIGN, 48>(p, bt, s);
     case 96: return launch_k<T, SIGN, 96>(p, bt, s);

@@ -14,7 +14,7 @@ int dmg_fft_pass_launch_f32(const dmg_fft_pass *p, const dmg_fft_batch *b, void 
   const int st = check_batch<float>(*p, *b);
   if (st != DMG_OK) return st;
   const bool inv = p->sign > 0;
-  if (pow2_group(p->n))
+  if (pow2_group(p->n) && !p->radix_runtime)
     return inv ? dmg_fft_pass_f32_inv_pow2(p, b, stream) : launch_pow2_group<float, -1>(*p, *b, stream);
   return inv ? dmg_fft_pass_f32_inv_mixed(p, b, stream) : dmg_fft_pass_f32_fwd_mixed(p, b, stream);
 }

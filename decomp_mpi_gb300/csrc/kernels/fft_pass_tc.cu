@@ -6,11 +6,11 @@
 int dmg_fft_pass_launch_f32(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream);
 
 size_t dmg_fft_pass_smem_tc(const dmg_fft_pass *p) {
-  return p->n == 1024 ? smem_layout<float>(*p, true, true).total : pass_smem<float>(*p);
+  return p->n == 1024 && !p->radix_runtime ? smem_layout<float>(*p, true, true).total : pass_smem<float>(*p);
 }
 
 int dmg_fft_pass_launch_tc(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream) {
-  if (p->n != 1024) return dmg_fft_pass_launch_f32(p, b, stream);
+  if (p->n != 1024 || p->radix_runtime) return dmg_fft_pass_launch_f32(p, b, stream);
   const int st = check_batch<float>(*p, *b);
   if (st != DMG_OK) return st;
   // a tile's lines make the products' 128 rows: at most four 1024-point lines

@@ -93,6 +93,20 @@ SplitPlan proposeParallelPlan(int flags, Decomp start, int *initial_factor, fftw
 /** Exhaustive search over factors and grids, timing each candidate on the
  * GPU (reference split_fft.h:54). */
 SplitPlan autotuneParallelPlan(Decomp start, fftw_complex *dat, int length, fftw_complex workspace[]);
+/** The autotuner for a given element type (DMG_C128 or DMG_C64); full_grid_search = 1 walks every
+ * processor grid of A and B as the reference does, 0 takes makeProcessorGrid's.  Besides the factors and
+ * the pass schedule it chooses the tile size and the radix schedules (dmg_split_set_tile,
+ * dmg_split_set_radix); winners are cached per (dimensions, lengths, virtual ranks, element type, grid
+ * search, start decomposition), and a cached choice is built without timing.  The search runs forward
+ * transforms over `dat` and `workspace`. */
+SplitPlan dmg_autotuneParallelPlanTyped(Decomp start, void *dat, long long length, void *workspace, int dtype,
+                                        int full_grid_search);
+/** Forget every cached autotuning winner. */
+void dmg_autotune_cache_clear(void);
+/** Number of cached autotuning winners. */
+int dmg_autotune_cache_entries(void);
+/** Configurations the last autotuning call timed (0 when it built a cached choice). */
+int dmg_autotune_last_timed(void);
 /** Slab (slab=1: last dim in stage 2 only) or balanced factors A <= B
  * (reference split_fft.h:55). */
 SplitPlan makeSplitPlan(int slab, Decomp start, fftw_complex *dat, int length, fftw_complex workspace[]);
@@ -183,6 +197,24 @@ int dmg_split_batch_launches(SplitPlan plan, int direction, int count);
 int dmg_split_set_schedule(SplitPlan plan, int schedule);
 /** The schedule in use: DMG_SCHEDULE_LINES or DMG_SCHEDULE_SPLIT. */
 int dmg_split_get_schedule(SplitPlan plan);
+/** Values per pass tile: 0 for the default (4096 for complex64, 2048 for
+ * complex128, the most), else a power of two from 64 up to that; smaller
+ * tiles hold fewer lines side by side. */
+int dmg_split_set_tile(SplitPlan plan, int values);
+/** The plan's values per tile. */
+int dmg_split_get_tile(SplitPlan plan);
+/* Radix schedules of the passes: DMG_RADIX_FIXED runs the compile-time
+ * schedules of the lengths that have one (powers of two 8...2048: radix 8
+ * stages, 16 as 4 x 4; the 2,3,5-smooth cube sides) and the plan's radices
+ * for the others; DMG_RADIX_PLAN8 and DMG_RADIX_PLAN4 run every pass with
+ * the plan's radices in the runtime-length kernel, 8s first or 4s first. */
+#define DMG_RADIX_FIXED 0
+#define DMG_RADIX_PLAN8 1
+#define DMG_RADIX_PLAN4 2
+/** Select the passes' radix schedules (DMG_RADIX_*). */
+int dmg_split_set_radix(SplitPlan plan, int radix);
+/** The plan's radix schedule choice. */
+int dmg_split_get_radix(SplitPlan plan);
 /** Status-returning run on an explicit stream (NULL = legacy default). */
 int dmg_split_run(SplitPlan plan, int direction, void *stream);
 /** Rebind the device buffers of a plan (same sizes). */

@@ -309,12 +309,12 @@ def test_cuda_graph_replay_matches_eager(dtype, cuda):
         assert np.array_equal(r.dat.cpu().numpy(), want_back)
 
 
-@pytest.mark.skip(reason="written before its first GB300 run; enabled once it has passed there")
 def test_autotune_small_cube(cuda):
     """autotuneParallelPlan (reference split_fft.c:78-247) on an 8x12x16 complex128 cube over a 2x2 grid:
-    it returns one of the makeParallelPlan plans in one of the two pass schedules; its forward transform
-    is the oracle's spectrum in that plan's slots, and has the same bits as makeParallelPlan with its
-    factors and schedule."""
+    it returns one of the makeParallelPlan plans in one of the two pass schedules, with a tile size and radix
+    schedule of its choice; its forward transform is the oracle's spectrum in that plan's slots, and has the
+    same bits as makeParallelPlan with its factors, schedule, tile and radix schedule.  A second call with the
+    same start decomposition builds the cached choice without timing."""
     import torch
     P, spec, shape = 4, "packed:local(8)|block(12,2)|block(16,2)", (8, 12, 16)
     comm = api.Comm(P)
@@ -326,7 +326,9 @@ def test_autotune_small_cube(cuda):
     dat = torch.from_numpy(host).to(cuda)
     work = torch.zeros(P * wl, dtype=torch.complex128, device=cuda)
     stream = torch.cuda.current_stream(cuda).cuda_stream
+    api.autotune_cache_clear()
     sp = api.SplitPlan(S, dat.data_ptr(), wl, work.data_ptr(), autotune=True)
+    assert api.autotune_last_timed() > 20 and api.autotune_cache_entries() == 1
     B = [L // a for L, a in zip(shape, sp.A_factors)]
     dat.copy_(torch.from_numpy(host))  # the search ran forward transforms over the buffers
     sp.run(api.FFTW_FORWARD, stream)
@@ -336,6 +338,58 @@ def test_autotune_small_cube(cuda):
     assert _rel(got[mask], exp[mask]) < TOL_C128
     work2 = torch.zeros_like(work)
     ref = api.SplitPlan(S, dat.data_ptr(), wl, work2.data_ptr(), B=B, schedule=sp.schedule)
+    ref.set_tile(sp.tile)
+    ref.set_radix(sp.radix)
     ref.run(api.FFTW_FORWARD, stream)
     torch.cuda.synchronize()
     assert np.array_equal(work2.cpu().numpy()[mask], got[mask])
+    # the cached choice
+    again = api.SplitPlan(S, dat.data_ptr(), wl, work2.data_ptr(), autotune=True)
+    assert api.autotune_last_timed() == 0
+    assert (again.A_factors, again.schedule, again.tile, again.radix) == (sp.A_factors, sp.schedule, sp.tile, sp.radix)
+
+
+@pytest.mark.parametrize("dtype", [api.C128, api.C64], ids=["c128", "c64"])
+def test_autotune_complex64_and_full_grid(dtype, cuda):
+    """The typed autotuner with the full grid search (every grid of A and B, as the reference walks them) on
+    a 2D array: the chosen plan's forward transform matches the oracle in the plan's own output slots."""
+    import torch
+    P, spec, shape = 4, "packed:block(8,2)|block(12,2)", (8, 12)
+    r = Run(P, spec, shape, cuda, dtype=dtype, seed=4)
+    tdt = torch.complex128 if dtype == api.C128 else torch.complex64
+    work = torch.zeros(P * r.wl, dtype=tdt, device=cuda)
+    sp = api.SplitPlan(r.S, r.dat.data_ptr(), r.wl, work.data_ptr(), autotune=True, dtype=dtype, full_grid=True)
+    assert api.autotune_last_timed() > 20
+    host = O.scatter_global(P, spec, r.glob, r.dp).astype(r.npdt)
+    r.dat.copy_(torch.from_numpy(host))
+    sp.run(api.FFTW_FORWARD, r.stream)
+    torch.cuda.synchronize()
+    got = work.cpu().numpy().astype(np.complex128)
+    # the chosen plan's B layout (its own grids) holds frequency k1 + B k2 in slot k2 + A k1 of each dimension
+    Bd = sp.decomp_B() or sp.decomp_A()
+    off = np.array([Bd.global_offset(c, r.wl) for c in np.ndindex(*shape)]).reshape(shape)
+    A = sp.A_factors
+    k = [np.arange(L) // a + (L // a) * (np.arange(L) % a) for L, a in zip(shape, A)]
+    want = O.fftn64(r.glob)[np.ix_(*k)]
+    tol = TOL_C128 if dtype == api.C128 else TOL_C64
+    assert _rel(got[off], want) < tol
+
+
+@pytest.mark.parametrize("tile,radix", [(1024, api.RADIX_FIXED), (512, api.RADIX_FIXED), (0, api.RADIX_PLAN8),
+                                        (0, api.RADIX_PLAN4), (256, api.RADIX_PLAN4)])
+@pytest.mark.parametrize("dtype", [api.C128, api.C64], ids=["c128", "c64"])
+def test_tile_and_radix_choices(tile, radix, dtype, cuda):
+    """Every tile size and radix schedule the autotuner may choose gives the oracle's forward spectrum and
+    the exact inverse."""
+    P, spec, shape = 16, "packed:block(48,4)|rotate(5,block(64,4))|local(32)", (48, 64, 32)
+    r = Run(P, spec, shape, cuda, dtype=dtype, seed=6)
+    r.plan.set_tile(tile)
+    r.plan.set_radix(radix)
+    assert r.plan.radix == radix
+    got = r.forward()
+    exp, mask = O.split_expected_output(P, spec, r.glob, r.wl)
+    tol = TOL_C128 if dtype == api.C128 else TOL_C64
+    assert _rel(got[mask].astype(np.complex128), exp[mask]) < tol
+    back = r.inverse()
+    g = O.gather_global(P, spec, back.astype(np.complex128), r.dp, r.shape) / np.prod(r.shape)
+    assert _rel(g, r.glob) < tol
