@@ -416,6 +416,8 @@ def run_gpu(args):
         torch.cuda.empty_cache()
         extras["served_stream"] = serve_study(args, njobs=args.jobs)
         torch.cuda.empty_cache()
+        extras["precision_form"] = precision_study(1024)
+        torch.cuda.empty_cache()
     cpu = cpu_baseline(args, reps=3)
     line = {
         "metric": "3D FFT GFLOP/s (5 N log2 N per transform) + reshape GB/s",
@@ -771,17 +773,18 @@ def run_serve(args):
     print(json.dumps(serve_study(args, args.jobs)))
 
 
-def run_precision(args):
-    """Precision form: 1024^3 complex64, complex Gaussian N(0,1) (seed 2) plus 16 unit-amplitude plane waves at
-    random wavenumbers (seed 2), on an 8x8 grid in the block decomposition.  Split 3D FFT forward in FP32; the
-    FP64-accuracy reference is the double-float complex128 transform of the same values on the GPU (pinned
-    against numpy's FP64 FFT to 1e-14 at smaller sizes); native FP64 is timed beside it."""
+def precision_study(n):
+    """Precision form: n^3 complex64 (n = 1024 in the benchmark), complex Gaussian N(0,1) (seed 2) plus 16
+    unit-amplitude plane waves at random wavenumbers (seed 2), on an 8x8 grid in the block decomposition.
+    Split 3D FFT forward in FP32 and in the tensor-core form (the 1024-point DFTs as FP16 hi + lo products
+    with FP32 accumulation); the FP64-accuracy reference is the double-float complex128 transform of the same
+    values on the GPU (the GPU tests pin the FP32 and tensor-core transforms against an FP64 oracle on the
+    host); native FP64 is timed beside it."""
     import numpy as np
     import torch
 
     from decomp_mpi_gb300 import api
 
-    n = args.n if args.n != N_SIDE else 1024
     g = 8
     Pp = g * g
     dev = torch.device("cuda:0")
@@ -903,13 +906,18 @@ def run_precision(args):
                         "arithmetic": "1024-point DFTs as two 32-point DFT products on the tensor cores: FP16 hi + lo "
                                       "operands, three products, FP32 accumulation, a power-of-two scale per row"},
     }
-    print(json.dumps(line))
+    return line
+
+
+def run_precision(args):
+    print(json.dumps(precision_study(args.n if args.n != N_SIDE else 1024)))
 
 
 def run_fft(args):
     """Split FFT alone: forward and inverse timings (CUDA events, median of 5 after 2 warm-up runs) and per-pass
-    times at n^3 on a g x g grid (--grid, 8 by default) in the factor_reverse decomposition of the headline chain,
-    for the chosen element type and every arithmetic and schedule that applies.  One JSON line."""
+    times at n^3 on a g x g grid (--grid, 8 by default) in the factor_reverse decomposition of the headline chain
+    (or, with --shape L0,L1,L2, in the block decomposition of that shape), for the chosen element type and every
+    arithmetic (or the one --arith names) and schedule that applies.  One JSON line."""
     import torch
 
     from decomp_mpi_gb300 import api
@@ -921,7 +929,11 @@ def run_fft(args):
     sh = stream.cuda_stream
     gs = args.grid
     P = gs * gs
-    _, _, frv = specs(n, (gs, gs))
+    if args.shape:
+        L = [int(x) for x in args.shape.split(",")]
+        frv = "packed:block(%d,%d)|block(%d,%d)|local(%d)" % (L[0], gs, L[1], gs, L[2])
+    else:
+        _, _, frv = specs(n, (gs, gs))
     comm = api.Comm(P)
     D = api.decomp_from_spec(comm, frv)
     tdt = torch.complex128 if dt == api.C128 else torch.complex64
@@ -935,9 +947,13 @@ def run_fft(args):
     probe.free()
     work = torch.empty(P * length, dtype=tdt, device=dev)
     sp = api.SplitPlan(D, dat.data_ptr(), length, work.data_ptr(), dtype=dt)
+    D_points = math.prod(int(x) for x in args.shape.split(",")) if args.shape else n ** 3
     scheds = {"lines": [api.SCHEDULE_LINES], "split": [api.SCHEDULE_SPLIT],
               "both": [api.SCHEDULE_LINES, api.SCHEDULE_SPLIT]}[args.schedule]
-    ariths = [api.ARITH_DF, api.ARITH_FP64] if dt == api.C128 else [api.ARITH_FP32]
+    ariths = [api.ARITH_DF, api.ARITH_FP64] if dt == api.C128 else [api.ARITH_FP32, api.ARITH_TC16]
+    if args.arith:
+        ariths = [{"fp64": api.ARITH_FP64, "df": api.ARITH_DF, "fp32": api.ARITH_FP32, "tc16": api.ARITH_TC16}[
+            args.arith]]
     out = {}
     for sched in scheds:
         try:
@@ -967,10 +983,11 @@ def run_fft(args):
             passes = sp.pass_times(api.FFTW_FORWARD)
             sp.set_timing(False)
             key = "%s/%s" % ("lines" if sched == api.SCHEDULE_LINES else "split",
-                             {api.ARITH_FP64: "fp64", api.ARITH_FP32: "fp32", api.ARITH_DF: "double-float"}[ar])
+                             {api.ARITH_FP64: "fp64", api.ARITH_FP32: "fp32", api.ARITH_DF: "double-float",
+                              api.ARITH_TC16: "tensor-core"}[ar])
             out[key] = {"forward_ms": round(statistics.median(f), 3), "inverse_ms": round(statistics.median(b), 3),
                         "forward_pass_ms": [round(x, 3) for x in passes],
-                        "forward_gflops": round(flops_per_transform(n ** 3) / (statistics.median(f) * 1e-3) / 1e9, 1)}
+                        "forward_gflops": round(flops_per_transform(D_points) / (statistics.median(f) * 1e-3) / 1e9, 1)}
             if n <= 128:
                 # small transforms are launch-bound: the same forward + inverse replayed from a CUDA graph
                 # (the plan's tables are on the device after the runs above, so capture allocates nothing)
@@ -1015,6 +1032,9 @@ def main():
     ap.add_argument("--dtype", default="c128", choices=["c128", "c64"], help="with --fft: element type")
     ap.add_argument("--grid", type=int, default=GRID[0], help="with --fft: virtual grid side (g x g ranks)")
     ap.add_argument("--schedule", default="both", choices=["lines", "split", "both"], help="with --fft")
+    ap.add_argument("--shape", default="", help="with --fft: L0,L1,L2 in the block decomposition instead of n^3")
+    ap.add_argument("--arith", default="", choices=["", "fp64", "df", "fp32", "tc16"],
+                    help="with --fft: that arithmetic only")
     ap.add_argument("--serve", action="store_true", help="served form: Poisson stream of mixed-size jobs")
     ap.add_argument("--precision", action="store_true", help="precision form: 1024^3 complex64 with error")
     ap.add_argument("--jobs", type=int, default=200, help="with --serve: jobs in the stream")
