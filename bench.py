@@ -655,7 +655,8 @@ def serve_study(args, njobs):
     """Served form: a Poisson stream (2000 req/s, seed 3) of block->rotate + split FFT forward + inverse jobs on
     a 4x4 virtual grid, sides from SERVE_SIDES, complex64 or complex128 with p = 1/2.  Runs the stream on the
     server (stream slots, admission by free HBM, same-shape batching), then the same jobs one at a time on a
-    one-slot server without batching ("alone"), and returns both."""
+    one-slot server without batching, in the same arithmetic ("alone") and with complex128 in native FP64, the
+    plain form ("alone_plain_fp64"), and returns all three."""
     import numpy as np
     import torch
 
@@ -717,22 +718,35 @@ def serve_study(args, njobs):
     lat = np.array([d["t_done"] - d["t_submit"] for d in done])
     batches = np.array([d["batch"] for d in done])
 
-    # alone: one slot, no batching, each job run by itself; latency as if the same arrivals queued for it
-    alone = make_server(1, 1)
-    for c in classes:
-        hi, hs, ho = bufs[c]
-        alone.submit(c[0], c[1], hi.data_ptr(), hs.data_ptr(), ho.data_ptr())
-    alone.drain()
-    alone.poll()
-    adone, aspan, aids = stream_run(alone, paced=False)
-    alone.close()
-    service = np.zeros(njobs)
-    for d in adone:
-        service[aids[d["id"]]] = d["t_done"] - d["t_start"]
-    finish, qlat = 0.0, np.zeros(njobs)
-    for i in range(njobs):
-        finish = max(arrivals[i], finish) + service[i]
-        qlat[i] = finish - arrivals[i]
+    def alone_run(arith128):
+        """One slot, no batching, each job run by itself (complex128 plans in `arith128`); per-job service times
+        and the latencies the same arrivals would see queueing for that one slot."""
+        alone = make_server(1, 1)
+        if arith128 is not None:
+            alone.set_arith(api.C128, arith128)
+        for c in classes:
+            hi, hs, ho = bufs[c]
+            alone.submit(c[0], c[1], hi.data_ptr(), hs.data_ptr(), ho.data_ptr())
+        alone.drain()
+        alone.poll()
+        adone, aspan, aids = stream_run(alone, paced=False)
+        alone.close()
+        service = np.zeros(njobs)
+        for d in adone:
+            service[aids[d["id"]]] = d["t_done"] - d["t_start"]
+        finish, qlat = 0.0, np.zeros(njobs)
+        for i in range(njobs):
+            finish = max(arrivals[i], finish) + service[i]
+            qlat[i] = finish - arrivals[i]
+        return {"busy_s": round(float(service.sum()), 4), "jobs_per_s": round(njobs / float(service.sum()), 2),
+                "gflops": round(flops / float(service.sum()) / 1e9, 2),
+                "p50_ms_same_arrivals": round(1e3 * float(np.percentile(qlat, 50)), 3),
+                "p99_ms_same_arrivals": round(1e3 * float(np.percentile(qlat, 99)), 3)}
+
+    # the same arithmetic one job at a time, and the plain form (complex128 in native FP64) one job at a time
+    alone_same = alone_run(None)
+    alone_plain = alone_run(api.ARITH_FP64)
+    served_rate = njobs / span
 
     # accuracy of the round trip per class (the inverse holds N times the rotated input)
     errs = {}
@@ -757,10 +771,12 @@ def serve_study(args, njobs):
                    "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 3),
                    "mean_batch": round(float(batches.mean()), 2), "max_batch": int(batches.max()),
                    "slots": args.slots, "max_batch_limit": args.batch, "arena_gib": args.arena_gb},
-        "alone": {"busy_s": round(float(service.sum()), 4), "jobs_per_s": round(njobs / float(service.sum()), 2),
-                  "gflops": round(flops / float(service.sum()) / 1e9, 2),
-                  "p50_ms_same_arrivals": round(1e3 * float(np.percentile(qlat, 50)), 3),
-                  "p99_ms_same_arrivals": round(1e3 * float(np.percentile(qlat, 99)), 3)},
+        "arithmetic": "served: complex128 in double-float, complex64 in FP32 (sides up to 512 have no 1024-point "
+                      "lines for the tensor-core stages)",
+        "alone": alone_same,
+        "alone_plain_fp64": alone_plain,
+        "served_over_alone": round(served_rate / alone_same["jobs_per_s"], 3),
+        "served_over_plain": round(served_rate / alone_plain["jobs_per_s"], 3),
         "roundtrip_rel_l2": errs,
         "config": {"grid": "4x4 virtual", "sides": SERVE_SIDES if not args.quick else SERVE_SIDES[:7],
                    "dtypes": "complex64 / complex128, p = 1/2", "seed": 3,

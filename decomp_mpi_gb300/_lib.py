@@ -122,6 +122,7 @@ SIGNATURES = {
     "dmg_decomp_scale": (_i, [_vp, _i, _vp, ctypes.POINTER(_vp), _i, _vp]),
     "dmg_visit_fill_index": (_i, [_vp, _i, _vp, _vp]),
     "dmg_server_create": (_vp, [_i, _ll, _i, _i]),
+    "dmg_server_set_arith": (_i, [_vp, _i, _i]),
     "dmg_server_job_sizes": (_i, [_vp, _i, _i, ctypes.POINTER(_ll), ctypes.POINTER(_ll), ctypes.POINTER(_ll)]),
     "dmg_server_submit": (_ll, [_vp, _vp]),
     "dmg_server_poll": (_i, [_vp, _vp, _i]),

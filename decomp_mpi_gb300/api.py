@@ -657,6 +657,11 @@ class Server:
             raise DecompError("dmg_server_create: %s" % last_error())
         self.grid = grid
 
+    def set_arith(self, dtype, arith):
+        """Arithmetic of the server's plans of one element type (C128: ARITH_DF or ARITH_FP64; C64: ARITH_FP32 or
+        ARITH_TC16); call it while no job is queued or running."""
+        check(self.lib.dmg_server_set_arith(self.h, int(dtype), int(arith)), "dmg_server_set_arith")
+
     def sizes(self, side, dtype):
         """Element counts of a job's host arrays: (input, spectrum, output)."""
         a, b, c = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()

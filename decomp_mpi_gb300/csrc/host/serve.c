@@ -65,6 +65,7 @@ typedef struct {
 
 struct dmg_server {
   int grid, P, nslots, max_batch, dev;
+  int arith[2]; /* arithmetic of complex128 and complex64 plans (DMG_ARITH_*; -1: the plan's default) */
   MPI_Comm comm;
   char *base;
   arena ar;
@@ -132,6 +133,9 @@ static plan_entry *plan_make(struct dmg_server *s, int side, int dtype) {
   pe->sp = dmg_makeSplitPlanTyped(0, pe->drot, (void *)(uintptr_t)ALIGN, pe->len, (void *)(uintptr_t)(2 * ALIGN),
                                   dtype);
   if (!pe->sp) goto fail;
+  if (s->arith[dtype == DMG_C128 ? 0 : 1] >= 0 &&
+      dmg_split_set_arith(pe->sp, s->arith[dtype == DMG_C128 ? 0 : 1]) != DMG_OK)
+    goto fail;
   pe->bytes_in = (long long)s->P * pe->pitch_blk * pe->es;
   pe->bytes_dat = (long long)s->P * pe->pitch_rot * pe->es;
   pe->bytes_work = (long long)s->P * pe->len * pe->es;
@@ -348,6 +352,7 @@ DmgServer dmg_server_create(int grid, long long arena_bytes, int slots, int max_
   if (!s) return NULL;
   s->grid = grid;
   s->P = grid * grid;
+  s->arith[0] = s->arith[1] = -1;
   s->nslots = slots;
   s->max_batch = max_batch;
   if (dmg_rt_get_device(&s->dev) != DMG_OK) goto fail;
@@ -375,6 +380,26 @@ DmgServer dmg_server_create(int grid, long long arena_bytes, int slots, int max_
 fail:
   dmg_server_destroy(s);
   return NULL;
+}
+
+int dmg_server_set_arith(DmgServer s, int dtype, int arith) {
+  if (!s || (dtype != DMG_C128 && dtype != DMG_C64))
+    return dmg_error(DMG_ERR_ARG, "dmg_server_set_arith: server %p, element type %d", (void *)s, dtype);
+  if (dtype == DMG_C128 ? (arith != DMG_ARITH_FP64 && arith != DMG_ARITH_DF)
+                        : (arith != DMG_ARITH_FP32 && arith != DMG_ARITH_TC16))
+    return dmg_error(DMG_ERR_ARG, "dmg_server_set_arith: arithmetic %d does not apply to element type %d", arith,
+                     dtype);
+  pthread_mutex_lock(&s->mu);
+  int st = DMG_OK;
+  if (s->running || s->nqueued) {
+    st = dmg_error(DMG_ERR_ARG, "dmg_server_set_arith: jobs are queued or running; drain the server first");
+  } else {
+    s->arith[dtype == DMG_C128 ? 0 : 1] = arith;
+    for (int i = 0; i < s->nplans && st == DMG_OK; ++i)
+      if (s->plans[i]->dtype == dtype) st = dmg_split_set_arith(s->plans[i]->sp, arith);
+  }
+  pthread_mutex_unlock(&s->mu);
+  return st;
 }
 
 int dmg_server_job_sizes(DmgServer s, int side, int dtype, long long *input, long long *spectrum,

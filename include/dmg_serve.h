@@ -52,6 +52,11 @@ typedef struct {
  * memory and `slots` streams; max_batch jobs at most share launches (1: no
  * batching).  NULL on failure. */
 DmgServer dmg_server_create(int grid, long long arena_bytes, int slots, int max_batch);
+/** Arithmetic of the server's plans of one element type: DMG_ARITH_DF (the
+ * default) or DMG_ARITH_FP64 for DMG_C128, DMG_ARITH_FP32 (the default) or
+ * DMG_ARITH_TC16 for DMG_C64.  Applies to cached plans too; refused while
+ * jobs are queued or running. */
+int dmg_server_set_arith(DmgServer s, int dtype, int arith);
 /** Element counts of a job's host arrays (input, spectrum, output). */
 int dmg_server_job_sizes(DmgServer s, int side, int dtype, long long *input, long long *spectrum, long long *output);
 /** Queue a job; returns its id (>= 0) or a negative error code.  A job that

@@ -208,3 +208,20 @@ def test_server_every_c5_side_both_types(sides, cuda):
         assert e_spec < TOL[dtype], (side, dtype, e_spec)
         assert e_back < TOL[dtype], (side, dtype, e_back)
     srv.close()
+
+
+def test_server_arithmetic_choice(cuda):
+    """dmg_server_set_arith: complex128 jobs in native FP64 and complex64 jobs in the tensor-core form give the
+    FP64 oracle's spectra and round trips; the choice is refused while jobs are queued."""
+    jobs = [(24, api.C128, 31), (32, api.C64, 32)]
+    srv = api.Server(GRID, 1 << 30, slots=2, max_batch=4)
+    srv.set_arith(api.C128, api.ARITH_FP64)
+    srv.set_arith(api.C64, api.ARITH_TC16)
+    with pytest.raises(Exception):
+        srv.set_arith(api.C128, api.ARITH_FP32)
+    bufs, _ = _run(srv, jobs, cuda, one_at_a_time=False)
+    for (side, dtype, seed), (hi, hs, ho) in zip(jobs, bufs):
+        g = _cube(side, dtype, seed).astype(np.complex128)
+        e_spec, e_back = _check_job(srv, side, dtype, g, hs, ho)
+        assert e_spec < TOL[dtype] and e_back < TOL[dtype], (side, dtype, e_spec, e_back)
+    srv.close()
