@@ -963,6 +963,8 @@ def run_fft(args):
     probe.free()
     work = torch.empty(P * length, dtype=tdt, device=dev)
     sp = api.SplitPlan(D, dat.data_ptr(), length, work.data_ptr(), dtype=dt)
+    if args.tile:
+        sp.set_tile(args.tile)
     D_points = math.prod(int(x) for x in args.shape.split(",")) if args.shape else n ** 3
     scheds = {"lines": [api.SCHEDULE_LINES], "split": [api.SCHEDULE_SPLIT],
               "both": [api.SCHEDULE_LINES, api.SCHEDULE_SPLIT]}[args.schedule]
@@ -1051,6 +1053,7 @@ def main():
     ap.add_argument("--shape", default="", help="with --fft: L0,L1,L2 in the block decomposition instead of n^3")
     ap.add_argument("--arith", default="", choices=["", "fp64", "df", "fp32", "tc16"],
                     help="with --fft: that arithmetic only")
+    ap.add_argument("--tile", type=int, default=0, help="with --fft: values per pass tile (0: the default)")
     ap.add_argument("--serve", action="store_true", help="served form: Poisson stream of mixed-size jobs")
     ap.add_argument("--precision", action="store_true", help="precision form: 1024^3 complex64 with error")
     ap.add_argument("--jobs", type=int, default=200, help="with --serve: jobs in the stream")

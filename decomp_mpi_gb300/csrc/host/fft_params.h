@@ -91,13 +91,27 @@ struct dmg_fft_pass {
   /* device word set to 1 when a tensor-core pass gave up waiting for its
    * products (NULL: not reported) */
   int32_t *status;
+  /* the tile holds more than DMG_FFT_TILE_TARGET values: the wide kernel */
+  int32_t wide;
 };
 
 /* Threads per pass block; the most values a tile may hold, and the number
  * the planner aims at (32 KB per tile buffer) for a value of es bytes. */
+#ifndef DMG_FFT_NT
 #define DMG_FFT_NT 256
+#endif
+#ifndef DMG_FFT_TILE_MAX
 #define DMG_FFT_TILE_MAX 4096
+#endif
+#ifndef DMG_FFT_TILE_TARGET
 #define DMG_FFT_TILE_TARGET(es) ((es) == 8 ? 4096 : 2048)
+#endif
+/* Wide passes: one 512-thread block per SM with tiles of twice the values,
+ * so that passes whose lines are strided in memory move rows twice as long
+ * (FP32 and double-float power-of-two lengths; the plan's tile size asks for
+ * them). */
+#define DMG_FFT_WIDE_NT 512
+#define DMG_FFT_WIDE_TILE(es) ((es) == 8 ? 8192 : 4096)
 
 /* Jobs of one batched launch: the same pass (same plan, so the same tables)
  * over several arrays.  scale_exp: per job, for double-float passes that

@@ -308,12 +308,23 @@ static int pass_geometry(const struct dmg_split_impl *im, struct dmg_fft_pass *p
   p->v2 = pick[1];
   p->nv1 = p->v1 >= 0 ? sub_len(A, B, p->v1) : 1;
   p->nv2 = p->v2 >= 0 ? sub_len(A, B, p->v2) : 1;
-  int room = (im->tile_values > 0 ? im->tile_values : DMG_FFT_TILE_TARGET(im->esize)) / p->n;
+  /* tile values: the plan's choice; more than the two-block kernels hold
+   * only for the wide kernels' case (FP32 or double-float, power-of-two
+   * length, compile-time radix schedule, not the tensor-core 1024-point
+   * stage, whose products take four lines) */
+  int target = im->tile_values > 0 ? im->tile_values : DMG_FFT_TILE_TARGET(im->esize);
+  const int pow2n = p->n >= 8 && p->n <= 2048 && (p->n & (p->n - 1)) == 0;
+  if (target > DMG_FFT_TILE_TARGET(im->esize) &&
+      (im->arith == DMG_ARITH_FP64 || !pow2n || im->radix != DMG_RADIX_FIXED ||
+       (im->arith == DMG_ARITH_TC16 && p->n == 1024)))
+    target = DMG_FFT_TILE_TARGET(im->esize);
+  int room = target / p->n;
   if (room < 1) room = 1;
   p->M1 = p->nv1 < room ? p->nv1 : room;
   room /= p->M1;
   if (room < 1) room = 1;
   p->M2 = p->nv2 < room ? p->nv2 : room;
+  p->wide = (int64_t)p->M1 * p->M2 * p->n > DMG_FFT_TILE_TARGET(im->esize);
   p->nt1 = (p->nv1 + p->M1 - 1) / p->M1;
   p->nt2 = (p->nv2 + p->M2 - 1) / p->M2;
   p->nbatch = 0;
@@ -1059,8 +1070,17 @@ int dmg_split_set_arith(SplitPlan plan, int arith) {
                            : (arith != DMG_ARITH_FP64 && arith != DMG_ARITH_DF))
     return dmg_error(DMG_ERR_ARG, "dmg_split_set_arith: arithmetic %d does not apply to this element type", arith);
   if (arith != im->arith) {
+    const int old = im->arith;
     im->arith = arith;
-    impl_free_device(im); /* tables differ between arithmetics */
+    /* the passes' tiles depend on the arithmetic (wide tiles), and the
+     * tables differ between arithmetics */
+    int st = build_passes(im);
+    if (st != DMG_OK) {
+      im->arith = old;
+      build_passes(im);
+      return st;
+    }
+    impl_free_device(im);
   }
   return DMG_OK;
 }
@@ -1115,7 +1135,7 @@ static int rebuild_with(struct dmg_split_impl *im, int *field, int value) {
 int dmg_split_set_tile(SplitPlan plan, int values) {
   if (!plan) return dmg_error(DMG_ERR_ARG, "dmg_split_set_tile: NULL plan");
   struct dmg_split_impl *im = plan->impl;
-  const int most = DMG_FFT_TILE_TARGET(im->esize);
+  const int most = DMG_FFT_WIDE_TILE(im->esize);
   if (values != 0 && (values < 64 || values > most || (values & (values - 1))))
     return dmg_error(DMG_ERR_ARG, "dmg_split_set_tile: %d values per tile (0, or a power of two from 64 to %d)",
                      values, most);

@@ -905,7 +905,9 @@ __device__ __forceinline__ void store_elem(void *dst, int64_t a, C2<T> v, bool f
 // transform-axis offsets are kept: two blocks per SM, each at most 112 KB
 // with its 1 KB reserve and static shared memory (measured: at 115 KB the
 // 1024-point FP32 passes fell to one block per SM)
+#ifndef DMG_FFT_T0_SMEM_LIMIT
 #define DMG_FFT_T0_SMEM_LIMIT 113328
+#endif
 
 // int64 entries of one side's separable address parts for a tile: unused,
 // M1 entries of v1's dimension, M2 of v2's, 3 of the dimensions no tile axis

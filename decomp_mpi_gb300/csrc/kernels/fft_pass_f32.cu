@@ -2,7 +2,11 @@
 // translation unit, and the forward direction's power-of-two lengths; see fft_pass.cuh.
 #include "fft_pass.cuh"
 
-size_t dmg_fft_pass_smem_f32(const dmg_fft_pass *p) { return pass_smem<float>(*p); }
+size_t dmg_fft_pass_smem_f32_wide(const dmg_fft_pass *p);
+int dmg_fft_pass_f32_wide(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream);
+int dmg_fft_pass_f32_inv_wide(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream);
+
+size_t dmg_fft_pass_smem_f32(const dmg_fft_pass *p) { return p->wide ? dmg_fft_pass_smem_f32_wide(p) : pass_smem<float>(*p); }
 
 // the other groups of lengths and the inverse direction (fft_pass_f32_inv.cu,
 // fft_pass_f32_mixed.cu, fft_pass_f32_inv_mixed.cu)
@@ -14,6 +18,7 @@ int dmg_fft_pass_launch_f32(const dmg_fft_pass *p, const dmg_fft_batch *b, void 
   const int st = check_batch<float>(*p, *b);
   if (st != DMG_OK) return st;
   const bool inv = p->sign > 0;
+  if (p->wide) return inv ? dmg_fft_pass_f32_inv_wide(p, b, stream) : dmg_fft_pass_f32_wide(p, b, stream);
   if (pow2_group(p->n) && !p->radix_runtime)
     return inv ? dmg_fft_pass_f32_inv_pow2(p, b, stream) : launch_pow2_group<float, -1>(*p, *b, stream);
   return inv ? dmg_fft_pass_f32_inv_mixed(p, b, stream) : dmg_fft_pass_f32_fwd_mixed(p, b, stream);

@@ -198,8 +198,11 @@ int dmg_split_set_schedule(SplitPlan plan, int schedule);
 /** The schedule in use: DMG_SCHEDULE_LINES or DMG_SCHEDULE_SPLIT. */
 int dmg_split_get_schedule(SplitPlan plan);
 /** Values per pass tile: 0 for the default (4096 for complex64, 2048 for
- * complex128, the most), else a power of two from 64 up to that; smaller
- * tiles hold fewer lines side by side. */
+ * complex128), else a power of two from 64 up to twice that.  Smaller tiles
+ * hold fewer lines side by side; larger ones run the FP32 and double-float
+ * passes of power-of-two lengths in one 512-thread block per SM (other
+ * passes keep the default), so that passes whose lines are strided in memory
+ * move longer rows. */
 int dmg_split_set_tile(SplitPlan plan, int values);
 /** The plan's values per tile. */
 int dmg_split_get_tile(SplitPlan plan);

@@ -393,3 +393,30 @@ def test_tile_and_radix_choices(tile, radix, dtype, cuda):
     back = r.inverse()
     g = O.gather_global(P, spec, back.astype(np.complex128), r.dp, r.shape) / np.prod(r.shape)
     assert _rel(g, r.glob) < tol
+
+
+@pytest.mark.parametrize("schedule", [api.SCHEDULE_LINES, api.SCHEDULE_SPLIT], ids=["lines", "split"])
+@pytest.mark.parametrize("P,spec,shape", [
+    (16, "packed:block(48,4)|rotate(5,block(64,4))|local(32)", (48, 64, 32)),
+    (16, "packed:block(64,4)|block(16,4)|local(1024)", (64, 16, 1024)),
+    (64, "packed:frev(16,8,block(128,8))|rotate(3,block(64,8))|local(32)", (128, 64, 32)),
+])
+@pytest.mark.parametrize("dtype", [api.C128, api.C64], ids=["c128", "c64"])
+def test_wide_tiles(dtype, P, spec, shape, schedule, cuda):
+    """Tiles of twice the default values (the 512-thread wide kernels for the power-of-two lengths; the others
+    keep the default) give the oracle's spectrum and the exact inverse; complex64 also in the tensor-core form,
+    whose 1024-point passes keep four-line tiles."""
+    ariths = [None] if dtype == api.C128 else [api.ARITH_FP32, api.ARITH_TC16]
+    for ar in ariths:
+        r = Run(P, spec, shape, cuda, dtype=dtype, seed=8, arith=ar, schedule=schedule)
+        r.plan.set_tile(8192 if dtype == api.C64 else 4096)
+        got = r.forward()
+        exp, mask = O.split_expected_output(P, spec, r.glob, r.wl)
+        tol = TOL_C128 if dtype == api.C128 else TOL_C64
+        assert _rel(got[mask].astype(np.complex128), exp[mask]) < tol, ar
+        back = r.inverse()
+        g = O.gather_global(P, spec, back.astype(np.complex128), r.dp, r.shape) / np.prod(r.shape)
+        assert _rel(g, r.glob) < tol, ar
+    if dtype == api.C128:
+        with pytest.raises(Exception):
+            r.plan.set_tile(8192)
