@@ -15,8 +15,8 @@
  *
  * Beyond the reference's search, the tuner chooses how the device runs the
  * plan: each candidate is timed in both pass schedules where its lengths
- * allow both, and the winner is then tried with half-size tiles and with the
- * plan's own radix schedules in the runtime-length kernel (8s first and 4s
+ * allow both, and the winner is then tried with half- and double-size tiles
+ * and with the plan's own radix schedules in the runtime-length kernel (8s first and 4s
  * first) instead of the compile-time ones, keeping what is faster.
  *
  * Winners are cached per (dimensions, lengths, virtual ranks, element type,
@@ -31,6 +31,7 @@
 #include "dmg_internal.h"
 #include "split_fft.h"
 #include "k1_params.h"
+#include "fft_params.h"
 
 SplitPlan dmg_build_plan_typed(int flags, int use_first, int use_second, Decomp start, int ndim, int A[], int B[],
                                int L[], int grid_a[], int grid_b[], void *dat, long long length, void *workspace,
@@ -107,17 +108,20 @@ static int time_candidate(tune_ctx *c, SplitPlan cand) {
   return 0;
 }
 
-/* The winner with half-size tiles and with the runtime radix schedules:
- * keeps each change that is faster. */
+/* The winner with half-size and double-size (wide-kernel) tiles and with the
+ * runtime radix schedules: keeps each change that is faster. */
 static void refine(tune_ctx *c) {
   SplitPlan b = c->best;
   if (!b) return;
-  const int tile = dmg_split_get_tile(b);
-  if (dmg_split_set_tile(b, tile / 2) == DMG_OK) {
+  const int base = DMG_FFT_TILE_TARGET(c->dtype == DMG_C128 ? 16 : 8);
+  const int tiles[2] = {base / 2, 2 * base};
+  for (int i = 0; i < 2; ++i) {
+    const int keep = dmg_split_get_tile(b);
+    if (dmg_split_set_tile(b, tiles[i]) != DMG_OK) continue;
     float ms = 0;
     c->tried++;
     if (time_forward(c, b, &ms) == DMG_OK && ms > 0 && ms < c->best_ms) c->best_ms = ms;
-    else dmg_split_set_tile(b, 0);
+    else dmg_split_set_tile(b, keep);
   }
   const int radices[2] = {DMG_RADIX_PLAN8, DMG_RADIX_PLAN4};
   for (int i = 0; i < 2; ++i) {

@@ -314,6 +314,13 @@ static int pass_geometry(const struct dmg_split_impl *im, struct dmg_fft_pass *p
    * stage, whose products take four lines) */
   int target = im->tile_values > 0 ? im->tile_values : DMG_FFT_TILE_TARGET(im->esize);
   const int pow2n = p->n >= 8 && p->n <= 2048 && (p->n & (p->n - 1)) == 0;
+  /* by default, FP32 passes whose lines are strided on the load side (a
+   * vector axis lies closer in memory than the transform axis) take the wide
+   * tiles: twice the row length there made such passes about 6 % faster at
+   * 1024^3, while passes along contiguous lines ran slower in the wide kernel */
+  if (im->tile_values == 0 && im->esize == 8 && p->v1 >= 0 &&
+      sub_step(im, li, A, t) > sub_step(im, li, A, p->v1))
+    target = DMG_FFT_WIDE_TILE(im->esize);
   if (target > DMG_FFT_TILE_TARGET(im->esize) &&
       (im->arith == DMG_ARITH_FP64 || !pow2n || im->radix != DMG_RADIX_FIXED ||
        (im->arith == DMG_ARITH_TC16 && p->n == 1024)))
@@ -1142,10 +1149,7 @@ int dmg_split_set_tile(SplitPlan plan, int values) {
   return rebuild_with(im, &im->tile_values, values);
 }
 
-int dmg_split_get_tile(SplitPlan plan) {
-  if (!plan) return -1;
-  return plan->impl->tile_values > 0 ? plan->impl->tile_values : DMG_FFT_TILE_TARGET(plan->impl->esize);
-}
+int dmg_split_get_tile(SplitPlan plan) { return plan ? plan->impl->tile_values : -1; }
 
 int dmg_split_set_radix(SplitPlan plan, int radix) {
   if (!plan) return dmg_error(DMG_ERR_ARG, "dmg_split_set_radix: NULL plan");

@@ -73,7 +73,8 @@ extern "C" int dmg_fft_pass_launch_batch(const dmg_fft_pass *p, int dtype, const
   const int64_t most = p->wide ? 2 * DMG_FFT_TILE_MAX : DMG_FFT_TILE_MAX;
   if ((int64_t)p->M1 * p->M2 * p->n > most)
     return dmg_error(DMG_ERR_ARG, "fft tile %d exceeds %lld", p->M1 * p->M2 * p->n, (long long)most);
-  if (p->wide && (dtype == 0 || dtype == 3 || p->radix_runtime || p->n < 8 || p->n > 2048 || (p->n & (p->n - 1))))
+  if (p->wide && (dtype == 0 || (dtype == 3 && p->n == 1024) || p->radix_runtime || p->n < 8 || p->n > 2048 ||
+                  (p->n & (p->n - 1))))
     return dmg_error(DMG_ERR_ARG, "fft pass: wide tiles for length %d in arithmetic %d", p->n, dtype);
   if ((p->perm_in || p->perm_out) && (p->perm_a < 1 || p->perm_b < 1 || (int64_t)p->perm_a * p->perm_b != p->n))
     return dmg_error(DMG_ERR_ARG, "fft slot order %d x %d does not match length %d", p->perm_a, p->perm_b, p->n);

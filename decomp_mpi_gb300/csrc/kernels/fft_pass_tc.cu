@@ -5,8 +5,10 @@
 
 int dmg_fft_pass_launch_f32(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream);
 
+size_t dmg_fft_pass_smem_f32(const dmg_fft_pass *p);
+
 size_t dmg_fft_pass_smem_tc(const dmg_fft_pass *p) {
-  return p->n == 1024 && !p->radix_runtime ? smem_layout<float>(*p, true, true).total : pass_smem<float>(*p);
+  return p->n == 1024 && !p->radix_runtime ? smem_layout<float>(*p, true, true).total : dmg_fft_pass_smem_f32(p);
 }
 
 int dmg_fft_pass_launch_tc(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream) {

@@ -204,7 +204,9 @@ int dmg_split_get_schedule(SplitPlan plan);
  * passes keep the default), so that passes whose lines are strided in memory
  * move longer rows. */
 int dmg_split_set_tile(SplitPlan plan, int values);
-/** The plan's values per tile. */
+/** The plan's values per tile as set (0: the default, which gives FP32
+ * passes whose lines are strided in memory the wide tiles and the others
+ * the two-block kernels' tiles). */
 int dmg_split_get_tile(SplitPlan plan);
 /* Radix schedules of the passes: DMG_RADIX_FIXED runs the compile-time
  * schedules of the lengths that have one (powers of two 8...2048: radix 8
