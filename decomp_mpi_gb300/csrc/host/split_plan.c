@@ -310,15 +310,17 @@ static int pass_geometry(const struct dmg_split_impl *im, struct dmg_fft_pass *p
   p->nv2 = p->v2 >= 0 ? sub_len(A, B, p->v2) : 1;
   /* tile values: the plan's choice; more than the two-block kernels hold
    * only for the wide kernels' case (FP32 or double-float, power-of-two
-   * length, compile-time radix schedule, not the tensor-core 1024-point
-   * stage, whose products take four lines) */
+   * length from 256 to 2048, compile-time radix schedule, not the
+   * tensor-core 1024-point stage, whose products take four lines) */
   int target = im->tile_values > 0 ? im->tile_values : DMG_FFT_TILE_TARGET(im->esize);
-  const int pow2n = p->n >= 8 && p->n <= 2048 && (p->n & (p->n - 1)) == 0;
+  /* (the wide kernels' shared memory holds their tiles for lines of 256
+   * points or more; shorter lines pad and tabulate too much per tile) */
+  const int pow2n = p->n >= 256 && p->n <= 2048 && (p->n & (p->n - 1)) == 0;
   /* by default, FP32 passes whose lines are strided on the load side (a
    * vector axis lies closer in memory than the transform axis) take the wide
    * tiles: twice the row length there made such passes about 6 % faster at
    * 1024^3, while passes along contiguous lines ran slower in the wide kernel */
-  if (im->tile_values == 0 && im->esize == 8 && p->v1 >= 0 &&
+  if (im->tile_values == 0 && im->esize == 8 && pow2n && p->v1 >= 0 &&
       sub_step(im, li, A, t) > sub_step(im, li, A, p->v1))
     target = DMG_FFT_WIDE_TILE(im->esize);
   if (target > DMG_FFT_TILE_TARGET(im->esize) &&

@@ -200,7 +200,7 @@ int dmg_split_get_schedule(SplitPlan plan);
 /** Values per pass tile: 0 for the default (4096 for complex64, 2048 for
  * complex128), else a power of two from 64 up to twice that.  Smaller tiles
  * hold fewer lines side by side; larger ones run the FP32 and double-float
- * passes of power-of-two lengths in one 512-thread block per SM (other
+ * passes of power-of-two lengths 256...2048 in one 512-thread block per SM (other
  * passes keep the default), so that passes whose lines are strided in memory
  * move longer rows. */
 int dmg_split_set_tile(SplitPlan plan, int values);
