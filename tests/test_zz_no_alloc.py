@@ -63,6 +63,9 @@ CASES = [
     (4, "packed:block(64,2)|block(32,2)|local(16)", (64, 32, 16), api.C64, api.ARITH_FP32, api.SCHEDULE_LINES),
     (16, "packed:block(48,4)|rotate(5,block(48,4))|local(40)", (48, 48, 40), api.C64, api.ARITH_FP32,
      api.SCHEDULE_SPLIT),
+    # 1024-point lines in the tensor-core form, and 256-point strided lines in FP32's wide tiles
+    (4, "packed:block(8,2)|block(8,2)|local(1024)", (8, 8, 1024), api.C64, api.ARITH_TC16, api.SCHEDULE_LINES),
+    (4, "packed:local(256)|block(16,2)|block(8,2)", (256, 16, 8), api.C64, api.ARITH_FP32, api.SCHEDULE_LINES),
 ]
 
 
