@@ -72,6 +72,7 @@ SIGNATURES = {
     "runReshapePlan": (None, [_vp, _vp, _vp, _vp]),
     "checkReshapePlanBounds": (_i, [_vp, _i, _i, _i]),
     "dmg_reshape_run": (_i, [_vp, _vp, _vp, _vp]),
+    "dmg_reshape_run_group": (_i, [_i, _vp, _vp, _vp, _vp]),
     "dmg_reshape_set_pitch": (_i, [_vp, _ll, _ll]),
     "dmg_reshape_pitch": (_ll, [_vp, _i]),
     "dmg_reshape_bytes": (_ll, [_vp]),

@@ -317,6 +317,15 @@ class ReshapePlan:
             pass
 
 
+def reshape_group(plans, srcs, dsts, stream=None):
+    """dmg_reshape_run_group: several reshapes (any plans) in as few launches as their kernels allow."""
+    n = len(plans)
+    P = (ctypes.c_void_p * n)(*[p.h for p in plans])
+    S = (ctypes.c_void_p * n)(*srcs)
+    D = (ctypes.c_void_p * n)(*dsts)
+    check(load().dmg_reshape_run_group(n, P, S, D, ctypes.c_void_p(stream or 0)), "dmg_reshape_run_group")
+
+
 def _int_array(vals):
     return (ctypes.c_int * len(vals))(*[int(v) for v in vals])
 

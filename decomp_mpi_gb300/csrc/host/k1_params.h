@@ -41,11 +41,30 @@ struct dmg_k1_params {
   struct dmg_k1_side src, dst;
 };
 
+/* Several reshapes in one launch (any sizes and decompositions, each with
+ * both sides contiguous along its tile's first axis, all moving units of one
+ * size with the same ranked / separable sides): job j's tiles are numbered
+ * from first_tile = the sum of the earlier jobs' ntiles. */
+#define DMG_K1_MAXGROUP 16
+struct dmg_k1_group_job {
+  struct dmg_k1_params p;
+  const void *src;
+  void *dst;
+  int64_t first_tile;
+};
+struct dmg_k1_group {
+  int32_t count;
+  int64_t total_tiles;
+  struct dmg_k1_group_job job[DMG_K1_MAXGROUP];
+};
+
 #ifdef __cplusplus
 extern "C" {
 #endif
 /* Launch the permutation kernel; unit is 1, 2, 4, 8 or 16 bytes. */
 int dmg_k1_launch(const struct dmg_k1_params *p, int unit, const void *src, void *dst, void *stream);
+/* One launch over a group of reshapes (see dmg_k1_group). */
+int dmg_k1_launch_group(const struct dmg_k1_group *g, int unit, void *stream);
 #ifdef __cplusplus
 }
 #endif

@@ -625,6 +625,78 @@ int dmg_reshape_run(ReshapePlan plan, const void *src, void *dest, void *stream)
   return dmg_k1_launch(&im->kp, im->unit, src, dest, stream);
 }
 
+/* The kernel parameters and unit dmg_reshape_run would launch with for
+ * these buffers (the fused form when both pointers allow it); an error when
+ * the buffers do not fit the plan. */
+static int launch_choice(struct dmg_reshape_impl *im, const void *src, const void *dest,
+                         const struct dmg_k1_params **kp, int *unit) {
+  int v = im->fuse_v;
+  if (v > 1 && ((uintptr_t)src % (uintptr_t)(im->unit * v) == 0) &&
+      ((uintptr_t)dest % (uintptr_t)(im->unit * v) == 0)) {
+    im->kp_fused.src.ranked = im->kp_fused.dst.ranked = 0;
+    *kp = &im->kp_fused;
+    *unit = im->unit * v;
+    return DMG_OK;
+  }
+  if ((uintptr_t)src % (uintptr_t)im->unit || (uintptr_t)dest % (uintptr_t)im->unit)
+    return dmg_error(DMG_ERR_ARG, "dmg_reshape_run_group: buffers not aligned to %d bytes", im->unit);
+  *kp = &im->kp;
+  *unit = im->unit;
+  return DMG_OK;
+}
+
+int dmg_reshape_run_group(int count, const ReshapePlan *plans, const void *const *srcs, void *const *dests,
+                          void *stream) {
+  if (count < 0 || (count > 0 && (!plans || !srcs || !dests)))
+    return dmg_error(DMG_ERR_ARG, "dmg_reshape_run_group: %d jobs, NULL arrays", count);
+  struct dmg_k1_group *g = (struct dmg_k1_group *)calloc(1, sizeof(struct dmg_k1_group));
+  if (!g) return dmg_error(DMG_ERR_NOMEM, "dmg_reshape_run_group: out of host memory");
+  int gunit = 0, st = DMG_OK;
+  for (int j = 0; j <= count && st == DMG_OK; ++j) {
+    const struct dmg_k1_params *kp = NULL;
+    int unit = 0, direct = 0;
+    if (j < count) {
+      ReshapePlan pl = plans[j];
+      if (!pl || !pl->impl) {
+        st = dmg_error(DMG_ERR_ARG, "dmg_reshape_run_group: job %d has no plan", j);
+        break;
+      }
+      struct dmg_reshape_impl *im = pl->impl;
+      if (im->moved == 0) continue;
+      if (!srcs[j] || !dests[j] || srcs[j] == dests[j]) {
+        st = dmg_error(DMG_ERR_ARG, "dmg_reshape_run_group: job %d's buffers", j);
+        break;
+      }
+      if (!im->dev_valid && (st = plan_upload(im)) != DMG_OK) break;
+      if ((st = launch_choice(im, srcs[j], dests[j], &kp, &unit)) != DMG_OK) break;
+      direct = kp->load_fast == kp->store_fast && kp->e0 * kp->e1 <= 2048;
+    }
+    /* close the open group when this job cannot join it (or at the end) */
+    if (g->count > 0 && (j == count || !direct || unit != gunit || g->count == DMG_K1_MAXGROUP ||
+                         kp->src.ranked != g->job[0].p.src.ranked || kp->dst.ranked != g->job[0].p.dst.ranked)) {
+      st = g->count == 1 ? dmg_k1_launch(&g->job[0].p, gunit, g->job[0].src, g->job[0].dst, stream)
+                         : dmg_k1_launch_group(g, gunit, stream);
+      g->count = 0;
+      g->total_tiles = 0;
+      if (st != DMG_OK) break;
+    }
+    if (j == count) break;
+    if (!direct) {
+      st = dmg_k1_launch(kp, unit, srcs[j], dests[j], stream); /* the transposing kernel runs alone */
+      continue;
+    }
+    struct dmg_k1_group_job *gj = &g->job[g->count++];
+    gj->p = *kp;
+    gj->src = srcs[j];
+    gj->dst = dests[j];
+    gj->first_tile = g->total_tiles;
+    g->total_tiles += kp->ntiles;
+    gunit = unit;
+  }
+  free(g);
+  return st;
+}
+
 void runReshapePlan(MPI_Comm comm, ReshapePlan plan, void *src, void *dest) {
   (void)comm;
   dmg_reshape_run(plan, src, dest, dmg_current_stream());

@@ -222,14 +222,19 @@ static int launch_batch(struct dmg_server *s, slot *sl) {
   void *dats[DMG_FFT_MAXBATCH], *works[DMG_FFT_MAXBATCH];
   int *scales[DMG_FFT_MAXBATCH];
   int rc = DMG_OK;
+  ReshapePlan plans[DMG_FFT_MAXBATCH];
+  const void *ins[DMG_FFT_MAXBATCH];
   for (int i = 0; i < k && rc == DMG_OK; ++i) {
     char *in = s->base + jobs[i]->off_in;
     dats[i] = s->base + jobs[i]->off_dat;
     works[i] = s->base + jobs[i]->off_work;
     scales[i] = (int *)(s->base + jobs[i]->off_scale);
+    plans[i] = pe->r01;
+    ins[i] = in;
     rc = dmg_rt_copy_async(in, jobs[i]->j.input, (size_t)pe->bytes_in, 0, st);
-    if (rc == DMG_OK) rc = dmg_reshape_run(pe->r01, in, dats[i], st);
   }
+  /* every job's block -> rotate reshape in one launch */
+  if (rc == DMG_OK) rc = dmg_reshape_run_group(k, plans, ins, dats, st);
   if (rc == DMG_OK) rc = dmg_split_run_batch(pe->sp, FFTW_FORWARD, st, k, dats, works, scales);
   for (int i = 0; i < k && rc == DMG_OK; ++i)
     if (jobs[i]->j.spectrum)

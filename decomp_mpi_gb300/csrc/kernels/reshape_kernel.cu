@@ -235,77 +235,121 @@ __device__ __forceinline__ int64_t direct_addr(const dmg_k1_side &s, int64_t bas
 // Same fast axis on both sides: every thread moves its own elements straight
 // from source to destination, MAXITEMS loads in flight before the stores,
 // with no shared memory and no barrier.  Tiles run along ax0 (contiguous on
-// both sides) and ax1.
+// both sides) and ax1.  One tile of one array:
 template <typename U, bool SR, bool DR>
-__global__ void __launch_bounds__(NT, 4) k1_direct(const dmg_k1_params p, const U *__restrict__ src, U *__restrict__ dst) {
+__device__ __forceinline__ void direct_tile(const dmg_k1_params &p, const U *__restrict__ src, U *__restrict__ dst,
+                                            int64_t tile) {
   const int ax0 = p.ax0, ax1 = p.ax1;
   const int e0 = p.e0, e1 = p.e1;
   const int tid = threadIdx.x;
-  for (int64_t tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
-    int64_t t = tile;
-    const int t0 = (int)(t % p.nt0);
-    t /= p.nt0;
-    int t1 = 0;
-    if (ax1 >= 0) {
-      t1 = (int)(t % p.nt1);
-      t /= p.nt1;
-    }
-    int64_t sb = 0, db = 0;
-    int32_t rs = 0, rd = 0;
-    int64_t sbto[DMG_MAXAX], dbto[DMG_MAXAX];
-    int32_t bax[DMG_MAXAX];
-#pragma unroll
-    for (int b = 0; b < DMG_MAXAX; ++b) {
-      if (b < p.nbatch) {
-        const int a = p.batch_ax[b];
-        const int c = (int)(t % p.len[a]);
-        t /= p.len[a];
-        bax[b] = a;
-        if constexpr (SR) {
-          rs += __ldg(p.src.rk[a] + c);
-          sbto[b] = __ldg(p.src.tab[a] + c);
-        } else {
-          sb += __ldg(p.src.tab[a] + c);
-        }
-        if constexpr (DR) {
-          rd += __ldg(p.dst.rk[a] + c);
-          dbto[b] = __ldg(p.dst.tab[a] + c);
-        } else {
-          db += __ldg(p.dst.tab[a] + c);
-        }
-      }
-    }
-    if ((SR ? rs < 0 : sb < 0) || (DR ? rd < 0 : db < 0)) continue;
-    const int g0 = t0 * e0, g1 = t1 * e1;
-    const int lim0 = min(e0, p.len[ax0] - g0);
-    const int lim1 = ax1 >= 0 ? min(e1, p.len[ax1] - g1) : 1;
-    const int n = lim0 * lim1;
-    int q = tid / lim0, r = tid - q * lim0;
-    const int dq = NT / lim0, dr = NT - (NT / lim0) * lim0;
-    U v[MAXITEMS];
-    int64_t da[MAXITEMS];
-#pragma unroll
-    for (int j = 0; j < MAXITEMS; ++j) {
-      da[j] = -1;
-      if (tid + j * NT < n) {
-        int64_t d = direct_addr<DR>(p.dst, db, rd, dbto, bax, p.nbatch, ax0, ax1, g0 + r, g1 + q);
-        int64_t s = direct_addr<SR>(p.src, sb, rs, sbto, bax, p.nbatch, ax0, ax1, g0 + r, g1 + q);
-        if (d >= 0 && s >= 0) {
-          v[j] = src[s];
-          da[j] = d;
-        }
-      }
-      r += dr;
-      q += dq;
-      if (r >= lim0) {
-        r -= lim0;
-        q += 1;
-      }
-    }
-#pragma unroll
-    for (int j = 0; j < MAXITEMS; ++j)
-      if (da[j] >= 0) dst[da[j]] = v[j];
+  int64_t t = tile;
+  const int t0 = (int)(t % p.nt0);
+  t /= p.nt0;
+  int t1 = 0;
+  if (ax1 >= 0) {
+    t1 = (int)(t % p.nt1);
+    t /= p.nt1;
   }
+  int64_t sb = 0, db = 0;
+  int32_t rs = 0, rd = 0;
+  int64_t sbto[DMG_MAXAX], dbto[DMG_MAXAX];
+  int32_t bax[DMG_MAXAX];
+#pragma unroll
+  for (int b = 0; b < DMG_MAXAX; ++b) {
+    if (b < p.nbatch) {
+      const int a = p.batch_ax[b];
+      const int c = (int)(t % p.len[a]);
+      t /= p.len[a];
+      bax[b] = a;
+      if constexpr (SR) {
+        rs += __ldg(p.src.rk[a] + c);
+        sbto[b] = __ldg(p.src.tab[a] + c);
+      } else {
+        sb += __ldg(p.src.tab[a] + c);
+      }
+      if constexpr (DR) {
+        rd += __ldg(p.dst.rk[a] + c);
+        dbto[b] = __ldg(p.dst.tab[a] + c);
+      } else {
+        db += __ldg(p.dst.tab[a] + c);
+      }
+    }
+  }
+  if ((SR ? rs < 0 : sb < 0) || (DR ? rd < 0 : db < 0)) return;
+  const int g0 = t0 * e0, g1 = t1 * e1;
+  const int lim0 = min(e0, p.len[ax0] - g0);
+  const int lim1 = ax1 >= 0 ? min(e1, p.len[ax1] - g1) : 1;
+  const int n = lim0 * lim1;
+  int q = tid / lim0, r = tid - q * lim0;
+  const int dq = NT / lim0, dr = NT - (NT / lim0) * lim0;
+  U v[MAXITEMS];
+  int64_t da[MAXITEMS];
+#pragma unroll
+  for (int j = 0; j < MAXITEMS; ++j) {
+    da[j] = -1;
+    if (tid + j * NT < n) {
+      int64_t d = direct_addr<DR>(p.dst, db, rd, dbto, bax, p.nbatch, ax0, ax1, g0 + r, g1 + q);
+      int64_t s = direct_addr<SR>(p.src, sb, rs, sbto, bax, p.nbatch, ax0, ax1, g0 + r, g1 + q);
+      if (d >= 0 && s >= 0) {
+        v[j] = src[s];
+        da[j] = d;
+      }
+    }
+    r += dr;
+    q += dq;
+    if (r >= lim0) {
+      r -= lim0;
+      q += 1;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < MAXITEMS; ++j)
+    if (da[j] >= 0) dst[da[j]] = v[j];
+}
+
+template <typename U, bool SR, bool DR>
+__global__ void __launch_bounds__(NT, 4) k1_direct(const dmg_k1_params p, const U *__restrict__ src, U *__restrict__ dst) {
+  for (int64_t tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) direct_tile<U, SR, DR>(p, src, dst, tile);
+}
+
+// Several reshapes, of any sizes and decompositions, in one persistent
+// launch: the tiles of all jobs form one sequence (job j's tiles from
+// first_tile), and a block finds the job of each of its tiles.  Every job
+// moves units of the same size and has the same ranked / separable sides.
+template <typename U, bool SR, bool DR>
+__global__ void __launch_bounds__(NT, 4) k1_direct_group(const dmg_k1_group g) {
+  for (int64_t tile = blockIdx.x; tile < g.total_tiles; tile += gridDim.x) {
+    int j = 0;
+    while (j + 1 < g.count && tile >= g.job[j + 1].first_tile) ++j;
+    const dmg_k1_group_job &job = g.job[j];
+    direct_tile<U, SR, DR>(job.p, static_cast<const U *>(job.src), static_cast<U *>(job.dst), tile - job.first_tile);
+  }
+}
+
+template <typename U, bool SR, bool DR>
+int launch_direct_group(const dmg_k1_group &g, cudaStream_t stream) {
+  auto kern = k1_direct_group<U, SR, DR>;
+  int dev = 0, nsm = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, 0);
+  if (per_sm < 1) per_sm = 1;
+  int64_t grid = (int64_t)nsm * per_sm;
+  if (grid > g.total_tiles) grid = g.total_tiles;
+  if (grid < 1) return DMG_OK;
+  kern<<<(unsigned)grid, NT, 0, stream>>>(g);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return dmg_error(DMG_ERR_CUDA, "grouped reshape kernel launch: %s", cudaGetErrorString(e));
+  return DMG_OK;
+}
+
+template <typename U>
+int launch_group_unit(const dmg_k1_group &g, cudaStream_t stream) {
+  const bool sr = g.job[0].p.src.ranked, dr = g.job[0].p.dst.ranked;
+  if (sr && dr) return launch_direct_group<U, true, true>(g, stream);
+  if (sr) return launch_direct_group<U, true, false>(g, stream);
+  if (dr) return launch_direct_group<U, false, true>(g, stream);
+  return launch_direct_group<U, false, false>(g, stream);
 }
 
 template <typename U, bool SR, bool DR>
@@ -369,6 +413,28 @@ extern "C" int dmg_k1_launch(const dmg_k1_params *p, int unit, const void *src, 
     case 4: return launch_unit<uint32_t>(*p, src, dst, s);
     case 8: return launch_unit<uint2>(*p, src, dst, s);
     case 16: return launch_unit<uint4>(*p, src, dst, s);
+    default: return dmg_error(DMG_ERR_ARG, "reshape unit %d bytes unsupported", unit);
+  }
+}
+
+extern "C" int dmg_k1_launch_group(const dmg_k1_group *g, int unit, void *stream) {
+  if (g->count < 1 || g->count > DMG_K1_MAXGROUP)
+    return dmg_error(DMG_ERR_ARG, "grouped reshape: %d jobs (1 to %d)", g->count, DMG_K1_MAXGROUP);
+  for (int j = 0; j < g->count; ++j) {
+    const dmg_k1_params &p = g->job[j].p;
+    if (p.e0 * p.e1 > NT * MAXITEMS || p.load_fast != p.store_fast || p.src.ranked != g->job[0].p.src.ranked ||
+        p.dst.ranked != g->job[0].p.dst.ranked)
+      return dmg_error(DMG_ERR_ARG, "grouped reshape: job %d does not fit the group's kernel", j);
+    if (g->job[j].first_tile != (j ? g->job[j - 1].first_tile + g->job[j - 1].p.ntiles : 0))
+      return dmg_error(DMG_ERR_ARG, "grouped reshape: job %d's tiles do not follow job %d's", j, j - 1);
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  switch (unit) {
+    case 1: return launch_group_unit<u8x1>(*g, s);
+    case 2: return launch_group_unit<u16x1>(*g, s);
+    case 4: return launch_group_unit<uint32_t>(*g, s);
+    case 8: return launch_group_unit<uint2>(*g, s);
+    case 16: return launch_group_unit<uint4>(*g, s);
     default: return dmg_error(DMG_ERR_ARG, "reshape unit %d bytes unsupported", unit);
   }
 }

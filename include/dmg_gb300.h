@@ -49,6 +49,15 @@ int dmg_reshape_set_pitch(ReshapePlan plan, long long src_pitch, long long dest_
 /** Status-returning run on an explicit stream.  src and dest must not
  * overlap. */
 int dmg_reshape_run(ReshapePlan plan, const void *src, void *dest, void *stream);
+/** Several reshapes, each with its own plan (any sizes and decompositions)
+ * and buffers, enqueued on one stream: those whose data moves along one
+ * contiguous axis on both sides (every packed layout) and that move units of
+ * the same size share one persistent kernel launch, up to 16 per launch;
+ * the others launch alone.  Each result is bit-identical to dmg_reshape_run
+ * with the same plan and buffers.  No counterpart in the reference, where
+ * every rank runs its own reshape. */
+int dmg_reshape_run_group(int count, const ReshapePlan *plans, const void *const *srcs, void *const *dests,
+                          void *stream);
 /** Bytes one run reads plus writes (2 * elements moved * element size). */
 long long dmg_reshape_bytes(ReshapePlan plan);
 /** Number of elements one run moves. */

@@ -236,3 +236,40 @@ def test_cuda_graph_replay(cuda):
     plan.run(src.data_ptr(), want.data_ptr(), stream.cuda_stream)
     torch.cuda.synchronize()
     assert torch.equal(got, want)
+
+
+def test_grouped_reshapes_of_mixed_sizes(cuda):
+    """dmg_reshape_run_group: reshapes of different sizes, decompositions and element sizes, and one that
+    transposes the fast axis, enqueued together; the contiguous ones of one element size share a launch.
+    Every result equals the same plan's single run bit for bit."""
+    import torch
+    cases = [
+        (4, "packed:block(48,2)|block(48,2)|local(48)", "packed:rotate(16,block(48,2))|rotate(1,block(48,2))|local(48)",
+         16),
+        (16, "packed:block(64,4)|block(32,4)|local(96)", "packed:frev(8,8,block(64,4))|block(32,4)|local(96)", 16),
+        (16, "packed:block(120,4)|block(120,4)|local(120)",
+         "packed:rotate(40,block(120,4))|rotate(1,block(120,4))|local(120)", 16),
+        (4, "packed:block(32,2)|block(16,2)|local(64)", "packed:interleave(block(4,2),8)|local(16)|block(64,2)", 8),
+        (4, "axes:block(64,2)@1,1|block(48,2)@32,2", "axes:block(64,2)@24,1|block(48,2)@1,2", 16),  # transposes
+        (9, "packed:block(30,3)|block(21,3)|local(16)", "packed:local(30)|rotate(2,block(21,3))|block(16,3)", 8),
+    ]
+    plans, srcs, want, got, keep = [], [], [], [], []
+    st = torch.cuda.current_stream(cuda).cuda_stream
+    rng = np.random.default_rng(9)
+    for P, a, b, es in cases:
+        comm = api.Comm(P)
+        S, D = api.decomp_from_spec(comm, a), api.decomp_from_spec(comm, b)
+        pl = api.ReshapePlan(comm, es, S, D)
+        src = torch.from_numpy(rng.integers(0, 1 << 62, (P * pl.src_pitch * es) // 8)).to(cuda)
+        w = torch.full(((P * pl.dest_pitch * es) // 8,), -1, dtype=torch.int64, device=cuda)
+        g = torch.full_like(w, -1)
+        pl.run(src.data_ptr(), w.data_ptr(), st)
+        plans.append(pl)
+        srcs.append(src)
+        want.append(w)
+        got.append(g)
+        keep.append((comm, S, D))
+    api.reshape_group(plans, [x.data_ptr() for x in srcs], [x.data_ptr() for x in got], st)
+    torch.cuda.synchronize()
+    for i in range(len(cases)):
+        assert torch.equal(got[i], want[i]), cases[i][1]
