@@ -183,3 +183,37 @@ def test_measured_split_plan_form(dtype):
     assert [(p[0], p[1]) for p in passes] == [("2", "512"), ("1", "512"), ("0", "512")], d
     assert [(p[2], p[3]) for p in passes] == [("tab", "tab"), ("atb", "atb"), ("abt", "abt")], d
     assert "per value" not in d and "shared dim" not in d, d
+
+
+def test_tile_choices_in_the_pass_list():
+    """Host side of the tile choice: complex64 FP32 plans give the strided 1024-point passes wide tiles (eight
+    lines) by default and the contiguous one four; the tensor-core form keeps four lines on its 1024-point
+    passes; an explicit tile size applies to every pass; complex128 refuses twice its wide size."""
+    import re
+    comm = api.Comm(64)
+    D = api.decomp_from_spec(comm, "packed:block(1024,8)|block(1024,8)|local(1024)")
+    sp = api.SplitPlan(D, 1 << 20, 2 * 1024 ** 3 // 64 + 1024, 1 << 21, dtype=api.C64)
+
+    def lines():
+        return [int(x) for x in re.findall(r" x(\d+) v2", sp.describe())]
+
+    assert sp.tile == 0 and lines() == [4, 8, 8]
+    sp.set_arith(api.ARITH_TC16)
+    assert lines() == [4, 4, 4]
+    sp.set_arith(api.ARITH_FP32)
+    sp.set_tile(2048)
+    assert sp.tile == 2048 and lines() == [2, 2, 2]
+    sp.set_tile(8192)
+    assert lines() == [8, 8, 8]
+    for bad in (32, 3000, 16384):
+        with pytest.raises(Exception):
+            sp.set_tile(bad)
+    D2 = api.decomp_from_spec(comm, "packed:block(512,8)|block(512,8)|local(512)")
+    sp2 = api.SplitPlan(D2, 1 << 20, 2 * 512 ** 3 // 64 + 1024, 1 << 21)
+    sp2.set_tile(4096)
+    with pytest.raises(Exception):
+        sp2.set_tile(8192)
+    sp2.set_radix(api.RADIX_PLAN4)
+    assert sp2.radix == api.RADIX_PLAN4
+    with pytest.raises(Exception):
+        sp2.set_radix(7)
