@@ -418,6 +418,8 @@ def run_gpu(args):
         torch.cuda.empty_cache()
         extras["precision_form"] = precision_study(1024)
         torch.cuda.empty_cache()
+        extras["grouped_small"] = group_study()
+        torch.cuda.empty_cache()
     cpu = cpu_baseline(args, reps=3)
     line = {
         "metric": "3D FFT GFLOP/s (5 N log2 N per transform) + reshape GB/s",
@@ -929,6 +931,114 @@ def run_precision(args):
     print(json.dumps(precision_study(args.n if args.n != N_SIDE else 1024)))
 
 
+GROUP_SHAPES = [(32, 32, 32), (48, 40, 36), (64, 48, 32), (40, 40, 40), (24, 30, 36), (60, 48, 40), (72, 64, 48),
+                (80, 60, 50), (96, 64, 32), (30, 30, 30), (36, 48, 60), (45, 40, 32), (64, 64, 64), (50, 40, 30),
+                (96, 96, 48), (20, 24, 30)]
+
+
+def group_study(steps=20):
+    """Grouped form: the 16 uneven small arrays of GROUP_SHAPES (block decomposition on a 4x4 virtual grid,
+    uniform[-1,1) values, seed 5), each transformed forward and back per step, (a) one plan at a time with the
+    fixed radix schedules, (b) one plan at a time with the runtime radix schedule PLAN8, (c) all 16 in one
+    dmg_split_run_group call (one launch per pass index, PLAN8), each eager and replayed from a CUDA graph;
+    complex128 in native FP64 and complex64 in FP32.  CUDA events over `steps` steps after 3 warm-up steps."""
+    import torch
+
+    from decomp_mpi_gb300 import api
+
+    dev = torch.device("cuda:0")
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    gs, P = 4, 16
+    comm = api.Comm(P)
+    out = {"metric": "grouped small split 3D FFTs (forward + inverse): transforms per second",
+           "shapes": [list(s) for s in GROUP_SHAPES], "grid": "4x4 virtual", "steps": steps}
+    points = sum(math.prod(s) for s in GROUP_SHAPES)
+    flops = 2 * sum(flops_per_transform(math.prod(s)) for s in GROUP_SHAPES)
+    for dt, ar, name in ((api.C128, api.ARITH_FP64, "c128_fp64"), (api.C64, api.ARITH_FP32, "c64_fp32")):
+        tdt = torch.complex128 if dt == api.C128 else torch.complex64
+        gen = torch.Generator(device=dev)
+        gen.manual_seed(5)
+        keep, plans = [], []
+        for L in GROUP_SHAPES:
+            D = api.decomp_from_spec(comm, "packed:block(%d,%d)|block(%d,%d)|local(%d)" % (L[0], gs, L[1], gs, L[2]))
+            dat = torch.empty(P * D.extent(), dtype=tdt, device=dev)
+            dat.real.uniform_(-1, 1, generator=gen)
+            dat.imag.uniform_(-1, 1, generator=gen)
+            wl = 2 * int(math.prod(L))
+            work = torch.zeros(P * wl, dtype=tdt, device=dev)
+            sp = api.SplitPlan(D, dat.data_ptr(), wl, work.data_ptr(), dtype=dt, arith=ar)
+            keep.append((D, dat, work))
+            plans.append(sp)
+
+        def one_by_one(hs):
+            for sp in plans:
+                sp.run(api.FFTW_FORWARD, hs)
+            for sp in plans:
+                sp.run(api.FFTW_BACKWARD, hs)
+
+        def grouped(hs):
+            api.split_run_group(plans, api.FFTW_FORWARD, hs)
+            api.split_run_group(plans, api.FFTW_BACKWARD, hs)
+
+        def timed(fn):
+            for _ in range(3):
+                fn(sh)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(steps):
+                fn(sh)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            eager = e0.elapsed_time(e1) / steps
+            cap = torch.cuda.Stream(dev)
+            cap.wait_stream(stream)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=cap):
+                fn(torch.cuda.current_stream(dev).cuda_stream)
+            for _ in range(3):
+                g.replay()
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(steps):
+                g.replay()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            graph = e0.elapsed_time(e1) / steps
+            del g
+            return {"eager_ms": round(eager, 4), "graph_ms": round(graph, 4),
+                    "eager_transforms_per_s": round(2 * len(plans) / (eager * 1e-3), 1),
+                    "graph_transforms_per_s": round(2 * len(plans) / (graph * 1e-3), 1),
+                    "graph_gflops": round(flops / (graph * 1e-3) / 1e9, 1)}
+
+        res = {}
+        for sp in plans:
+            sp.set_radix(api.RADIX_FIXED)
+        res["one_by_one_fixed_radix"] = timed(one_by_one)
+        res["one_by_one_fixed_radix"]["launches"] = sum(sp.launches(api.FFTW_FORWARD) + sp.launches(api.FFTW_BACKWARD)
+                                                        for sp in plans)
+        for sp in plans:
+            sp.set_radix(api.RADIX_PLAN8)
+        res["one_by_one_plan8"] = timed(one_by_one)
+        res["grouped_plan8"] = timed(grouped)
+        res["grouped_plan8"]["launches"] = (api.split_group_launches(plans, api.FFTW_FORWARD) +
+                                            api.split_group_launches(plans, api.FFTW_BACKWARD))
+        res["grouped_over_one_by_one_fixed"] = {
+            k: round(res["one_by_one_fixed_radix"][k] / res["grouped_plan8"][k], 3) for k in ("eager_ms", "graph_ms")}
+        out[name] = res
+        for sp in plans:
+            sp.free()
+        del keep
+        torch.cuda.empty_cache()
+    out["points_per_step"] = 2 * points
+    return out
+
+
+def run_group(args):
+    print(json.dumps(group_study(max(args.steps, 10))))
+
+
 def run_fft(args):
     """Split FFT alone: forward and inverse timings (CUDA events, median of 5 after 2 warm-up runs) and per-pass
     times at n^3 on a g x g grid (--grid, 8 by default) in the factor_reverse decomposition of the headline chain
@@ -1056,6 +1166,7 @@ def main():
     ap.add_argument("--tile", type=int, default=0, help="with --fft: values per pass tile (0: the default)")
     ap.add_argument("--serve", action="store_true", help="served form: Poisson stream of mixed-size jobs")
     ap.add_argument("--precision", action="store_true", help="precision form: 1024^3 complex64 with error")
+    ap.add_argument("--group", action="store_true", help="grouped form: 16 uneven small transforms per launch")
     ap.add_argument("--jobs", type=int, default=200, help="with --serve: jobs in the stream")
     ap.add_argument("--rate", type=float, default=2000.0, help="with --serve: mean arrivals per second")
     ap.add_argument("--slots", type=int, default=4, help="with --serve: stream slots")
@@ -1068,7 +1179,7 @@ def main():
     if args.impl == "reference":
         run_reference(args)
         return
-    if not (args.sweep or args.fft or args.serve or args.precision):
+    if not (args.sweep or args.fft or args.serve or args.precision or args.group):
         run_gpu(args)  # every rank: one replica of the workload per GPU
         return
     if int(os.environ.get("WORLD_SIZE", "1")) > 1 and int(os.environ.get("RANK", "0")) != 0:
@@ -1084,6 +1195,9 @@ def main():
         return
     if args.precision:
         run_precision(args)
+        return
+    if args.group:
+        run_group(args)
         return
 
 

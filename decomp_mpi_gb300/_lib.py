@@ -119,6 +119,8 @@ SIGNATURES = {
     "dmg_split_set_schedule": (_i, [_vp, _i]),
     "dmg_split_run_batch": (_i, [_vp, _i, _vp, _i, _vp, _vp, _vp]),
     "dmg_split_batch_launches": (_i, [_vp, _i, _i]),
+    "dmg_split_run_group": (_i, [_i, _vp, _i, _vp]),
+    "dmg_split_group_launches": (_i, [_i, _vp, _i]),
     "dmg_split_extent64": (_ll, [_vp]),
     "dmg_decomp_scale": (_i, [_vp, _i, _vp, ctypes.POINTER(_vp), _i, _vp]),
     "dmg_visit_fill_index": (_i, [_vp, _i, _vp, _vp]),

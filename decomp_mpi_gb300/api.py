@@ -527,6 +527,20 @@ class SplitPlan:
             pass
 
 
+def split_run_group(plans, direction, stream=None):
+    """dmg_split_run_group: runSplitPlan on several plans (any sizes; runtime radix schedules, one arithmetic),
+    the k-th passes of all of them in one launch."""
+    n = len(plans)
+    P = (ctypes.c_void_p * n)(*[p.h for p in plans])
+    check(load().dmg_split_run_group(n, P, int(direction), ctypes.c_void_p(stream or 0)), "dmg_split_run_group")
+
+
+def split_group_launches(plans, direction) -> int:
+    n = len(plans)
+    P = (ctypes.c_void_p * n)(*[p.h for p in plans])
+    return load().dmg_split_group_launches(n, P, int(direction))
+
+
 def autotune_cache_clear():
     """Forget every cached autotuning winner."""
     load().dmg_autotune_cache_clear()

@@ -124,9 +124,27 @@ struct dmg_fft_batch {
   const int32_t *scale_exp[DMG_FFT_MAXBATCH];
 };
 
+/* Passes of different plans (any lengths; each pass run by the
+ * runtime-length stages) in one launch: job j's pass runs on blocks
+ * first_block .. first_block + nblocks - 1 of the grid as if they were its
+ * own launch (the launcher fills in first_block and nblocks). */
+#define DMG_FFT_MAXGROUP 16
+struct dmg_fft_group_job {
+  struct dmg_fft_pass p;
+  struct dmg_fft_batch bt;
+  int64_t first_block, nblocks;
+};
+struct dmg_fft_group {
+  int32_t count;
+  struct dmg_fft_group_job job[DMG_FFT_MAXGROUP];
+};
+
 #ifdef __cplusplus
 extern "C" {
 #endif
+/* One launch over a group of passes of one arithmetic (dtype as below) and
+ * direction, each with radix_runtime set. */
+int dmg_fft_pass_launch_group(const struct dmg_fft_group *g, int dtype, void *stream);
 /* One launch of a pass over every job of a batch (the tiles of all jobs
  * share the persistent blocks). */
 int dmg_fft_pass_launch_batch(const struct dmg_fft_pass *p, int dtype, const struct dmg_fft_batch *b, void *stream);

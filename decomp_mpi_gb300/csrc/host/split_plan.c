@@ -1315,6 +1315,90 @@ int dmg_split_batch_launches(SplitPlan plan, int direction, int count) {
   return k;
 }
 
+/* ---------------------------------------------------------------- grouped run */
+
+_Static_assert(DMG_SPLIT_MAXGROUP == DMG_FFT_MAXGROUP, "a group is one launch per pass");
+
+/* The k-th passes of several plans (any sizes, decompositions and pass
+ * counts) in one launch each: plan i's pass k reads what its pass k-1 wrote
+ * in the launch before, on the same stream.  Every plan runs its passes with
+ * the runtime stages of its radix schedule, so it must have one
+ * (DMG_RADIX_PLAN8 or DMG_RADIX_PLAN4); its results are then the bits of
+ * dmg_split_run on the same plan. */
+static int group_check(int count, SplitPlan const *plans, int direction, const char *who) {
+  if (direction != FFTW_FORWARD && direction != FFTW_BACKWARD)
+    return dmg_error(DMG_ERR_ARG, "%s: direction %d", who, direction);
+  if (count < 1 || count > DMG_FFT_MAXGROUP)
+    return dmg_error(DMG_ERR_ARG, "%s: %d plans (1 to %d)", who, count, DMG_FFT_MAXGROUP);
+  for (int i = 0; i < count; ++i) {
+    if (!plans[i]) return dmg_error(DMG_ERR_ARG, "%s: NULL plan %d", who, i);
+    const struct dmg_split_impl *im = plans[i]->impl;
+    if (!im->dat || !im->work) return dmg_error(DMG_ERR_ARG, "%s: NULL buffer in plan %d", who, i);
+    if (im->radix == DMG_RADIX_FIXED)
+      return dmg_error(DMG_ERR_ARG, "%s: plan %d has the fixed radix schedules; set DMG_RADIX_PLAN8 or "
+                                    "DMG_RADIX_PLAN4 on every plan of a group", who, i);
+    if (im->nfwd == 0) return dmg_error(DMG_ERR_UNSUPPORTED, "%s: plan %d has no transform passes", who, i);
+    if (arith_dtype(im) != arith_dtype(plans[0]->impl))
+      return dmg_error(DMG_ERR_ARG, "%s: plan %d's arithmetic differs from plan 0's", who, i);
+    for (int j = 0; j < i; ++j)
+      if (plans[j] == plans[i]) return dmg_error(DMG_ERR_ARG, "%s: plan %d appears twice", who, i);
+  }
+  return DMG_OK;
+}
+
+int dmg_split_run_group(int count, SplitPlan const *plans, int direction, void *stream) {
+  if (!plans) return dmg_error(DMG_ERR_ARG, "dmg_split_run_group: NULL plan list");
+  int st = group_check(count, plans, direction, "dmg_split_run_group");
+  if (st != DMG_OK) return st;
+  int most = 0;
+  for (int i = 0; i < count; ++i) {
+    struct dmg_split_impl *im = plans[i]->impl;
+    if (!im->dev_valid && (st = impl_upload(im)) != DMG_OK) return st;
+    const int cnt = direction == FFTW_FORWARD ? im->nfwd : im->ninv;
+    if (cnt > most) most = cnt;
+    if (im->arith == DMG_ARITH_DF) {
+      const pass_rec *first = direction == FFTW_FORWARD ? &im->fwd[0] : &im->inv[0];
+      st = launch_maxexp(im, first, first->in_buf == BUF_DAT ? im->dat : im->work, stream);
+      if (st != DMG_OK) return st;
+    }
+  }
+  /* the group's descriptor is about 16 KB: keep it off the stack */
+  struct dmg_fft_group *g = (struct dmg_fft_group *)calloc(1, sizeof(struct dmg_fft_group));
+  if (!g) return dmg_error(DMG_ERR_NOMEM, "dmg_split_run_group: out of memory");
+  const int dt = arith_dtype(plans[0]->impl);
+  for (int k = 0; k < most && st == DMG_OK; ++k) {
+    g->count = 0;
+    for (int i = 0; i < count; ++i) {
+      struct dmg_split_impl *im = plans[i]->impl;
+      const int cnt = direction == FFTW_FORWARD ? im->nfwd : im->ninv;
+      if (k >= cnt) continue;
+      const pass_rec *r = direction == FFTW_FORWARD ? &im->fwd[k] : &im->inv[k];
+      struct dmg_fft_group_job *job = &g->job[g->count++];
+      memset(job, 0, sizeof(*job));
+      job->p = r->p;
+      job->bt.count = 1;
+      job->bt.src[0] = r->in_buf == BUF_DAT ? im->dat : im->work;
+      job->bt.dst[0] = r->out_buf == BUF_DAT ? im->dat : im->work;
+      job->bt.scale_exp[0] = r->p.scale_exp;
+    }
+    st = dmg_fft_pass_launch_group(g, dt, stream);
+  }
+  free(g);
+  return st;
+}
+
+int dmg_split_group_launches(int count, SplitPlan const *plans, int direction) {
+  if (!plans || group_check(count, plans, direction, "dmg_split_group_launches") != DMG_OK) return 0;
+  int most = 0, pre = 0;
+  for (int i = 0; i < count; ++i) {
+    const struct dmg_split_impl *im = plans[i]->impl;
+    const int cnt = direction == FFTW_FORWARD ? im->nfwd : im->ninv;
+    if (cnt > most) most = cnt;
+    if (im->arith == DMG_ARITH_DF) pre += 1; /* the exponent pre-pass, per plan */
+  }
+  return most + pre;
+}
+
 
 
 /* ---------------------------------------------------------------- no-allocation run */

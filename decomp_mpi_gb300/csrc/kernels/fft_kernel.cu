@@ -12,6 +12,13 @@ int dmg_fft_pass_launch_tc(const dmg_fft_pass *p, const dmg_fft_batch *b, void *
 int dmg_fft_pass_launch_f64(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream);
 int dmg_fft_pass_launch_f32(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream);
 int dmg_fft_pass_launch_df(const dmg_fft_pass *p, const dmg_fft_batch *b, void *stream);
+// grouped runtime-length passes (fft_pass_*_mixed.cu)
+int dmg_fft_pass_f64_fwd_group(const dmg_fft_group *g, void *stream);
+int dmg_fft_pass_f64_inv_group(const dmg_fft_group *g, void *stream);
+int dmg_fft_pass_f32_fwd_group(const dmg_fft_group *g, void *stream);
+int dmg_fft_pass_f32_inv_group(const dmg_fft_group *g, void *stream);
+int dmg_fft_pass_df_fwd_group(const dmg_fft_group *g, void *stream);
+int dmg_fft_pass_df_inv_group(const dmg_fft_group *g, void *stream);
 
 namespace {
 
@@ -83,6 +90,33 @@ extern "C" int dmg_fft_pass_launch_batch(const dmg_fft_pass *p, int dtype, const
     case 1: return dmg_fft_pass_launch_f32(p, b, stream);
     case 2: return dmg_fft_pass_launch_df(p, b, stream);
     case 3: return dmg_fft_pass_launch_tc(p, b, stream);
+    default: return dmg_error(DMG_ERR_ARG, "fft dtype %d", dtype);
+  }
+}
+
+extern "C" int dmg_fft_pass_launch_group(const dmg_fft_group *g, int dtype, void *stream) {
+  if (g->count < 1 || g->count > DMG_FFT_MAXGROUP)
+    return dmg_error(DMG_ERR_ARG, "grouped fft pass: %d passes (1 to %d)", g->count, DMG_FFT_MAXGROUP);
+  const int sign = g->job[0].p.sign;
+  for (int j = 0; j < g->count; ++j) {
+    const dmg_fft_pass &p = g->job[j].p;
+    if (!p.radix_runtime || p.wide || p.sign != sign)
+      return dmg_error(DMG_ERR_ARG, "grouped fft pass %d: needs runtime stages, plain tiles and one direction", j);
+    if ((int64_t)p.M1 * p.M2 * p.n > DMG_FFT_TILE_MAX)
+      return dmg_error(DMG_ERR_ARG, "fft tile %d exceeds %d", p.M1 * p.M2 * p.n, DMG_FFT_TILE_MAX);
+    if ((p.perm_in || p.perm_out) && (p.perm_a < 1 || p.perm_b < 1 || (int64_t)p.perm_a * p.perm_b != p.n))
+      return dmg_error(DMG_ERR_ARG, "fft slot order %d x %d does not match length %d", p.perm_a, p.perm_b, p.n);
+    const int st = dtype == 0 ? check_batch<double>(p, g->job[j].bt)
+                              : dtype == 2 ? check_batch<df>(p, g->job[j].bt) : check_batch<float>(p, g->job[j].bt);
+    if (st != DMG_OK) return st;
+  }
+  const bool inv = sign > 0;
+  switch (dtype) {
+    case 0: return inv ? dmg_fft_pass_f64_inv_group(g, stream) : dmg_fft_pass_f64_fwd_group(g, stream);
+    case 1:
+    case 3:  // the tensor-core form has no runtime-length kernel: its passes run in FP32
+      return inv ? dmg_fft_pass_f32_inv_group(g, stream) : dmg_fft_pass_f32_fwd_group(g, stream);
+    case 2: return inv ? dmg_fft_pass_df_inv_group(g, stream) : dmg_fft_pass_df_fwd_group(g, stream);
     default: return dmg_error(DMG_ERR_ARG, "fft dtype %d", dtype);
   }
 }

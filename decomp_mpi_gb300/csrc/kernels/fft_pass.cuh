@@ -1628,8 +1628,11 @@ __device__ __forceinline__ const float2 *tc_finish(unsigned char *A, uint32_t a_
 
 // NF > 0: length NF with a compile-time schedule; NF == 0: any length.
 // TC: the 1024-point FP32 pass with its DFT on the tensor cores (see above).
+// The pass as block `bid` of `nblk` persistent blocks (a launch's grid, or a
+// job's share of a grouped launch).
 template <typename T, int SIGN, int NF, bool TC = false>
-__global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p, const dmg_fft_batch bt) {
+__device__ __forceinline__ void pass_body(const dmg_fft_pass &p, const dmg_fft_batch &bt, const int64_t bid,
+                                          const int64_t nblk) {
   static_assert(!TC || (std::is_same<T, float>::value && NF == 1024), "tensor-core stages: 1024-point FP32");
   constexpr bool FIXED = NF > 0;
   // power-of-two lengths: buffers at compile-time offsets (staging, A, B, twiddle tables)
@@ -1670,12 +1673,12 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
     kc.rad[1] = p.nt2;
     for (int b = 0; b < p.nbatch; ++b) kc.rad[2 + b] = p.blen[b];
     kc.rad[2 + p.nbatch] = bt.count;
-    tile_digits(kc.rad, nd, blockIdx.x, kc.dig);
-    tile_digits(kc.rad, nd, gridDim.x, kc.inc);
-    if (blockIdx.x < ntiles_all) {
+    tile_digits(kc.rad, nd, bid, kc.dig);
+    tile_digits(kc.rad, nd, nblk, kc.inc);
+    if (bid < ntiles_all) {
       tile_state_digits<T>(p, bt, kc.dig, kc.ts[0]);
       digits_add(kc.dig, kc.inc, kc.rad, nd);
-      if (blockIdx.x + gridDim.x < ntiles_all) tile_state_digits<T>(p, bt, kc.dig, kc.ts[1]);
+      if (bid + nblk < ntiles_all) tile_state_digits<T>(p, bt, kc.dig, kc.ts[1]);
     }
     if constexpr (TC) {
       kc.tc_fail = 0;
@@ -1730,7 +1733,7 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
       if (kc.t0_out)
         for (int i = tid; i < n; i += NT) t0o[i] = (int32_t)(__ldg(p.out.tab[d0] + i * m0) - kc.t0base_out);
     }
-    if (blockIdx.x < ntiles_all) {
+    if (bid < ntiles_all) {
       const TileState &st = kc.ts[0];
       if (p.sep_in || p.semi_in) sep_parts_async(p.in, p, st.yb, st.zb, st.lim1, st.lim2, tid, parts_in, p.semi_in);
       if (p.sep_out || p.semi_out)
@@ -1740,17 +1743,17 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
   }
   copy_async_wait_all();
   __syncthreads();
-  if (blockIdx.x < ntiles_all) gather_async<T, NF>(p, kc, kc.ts[0], sm, parts_in, bt, tid);
+  if (bid < ntiles_all) gather_async<T, NF>(p, kc, kc.ts[0], sm, parts_in, bt, tid);
 
   int it = 0;
-  for (int64_t tile = blockIdx.x; tile < ntiles_all; tile += gridDim.x, ++it) {
-    const int64_t next = tile + gridDim.x;
+  for (int64_t tile = bid; tile < ntiles_all; tile += nblk, ++it) {
+    const int64_t next = tile + nblk;
     const int cur = it % 3, nxt = (it + 1) % 3;  // state slots of this tile and the next
     // ---- the tile's values are in the staging buffer ----
     copy_async_wait_all();
     __syncthreads();
     // the state of the tile after the next (read after later barriers)
-    if (tid == 0 && next + gridDim.x < ntiles_all) {
+    if (tid == 0 && next + nblk < ntiles_all) {
       digits_add(kc.dig, kc.inc, kc.rad, kc.ndig);
       tile_state_digits<T>(p, bt, kc.dig, kc.ts[(it + 2) % 3]);
     }
@@ -1949,6 +1952,61 @@ __global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p
     if (tid < 32) tc::tmem_dealloc(kc.tc_taddr, 64);
     if (tid == 0 && kc.tc_fail && p.status) atomicExch(p.status, 1);
   }
+}
+
+template <typename T, int SIGN, int NF, bool TC = false>
+__global__ void __launch_bounds__(NT, MINB) fft_pass_kernel(const dmg_fft_pass p, const dmg_fft_batch bt) {
+  pass_body<T, SIGN, NF, TC>(p, bt, blockIdx.x, gridDim.x);
+}
+
+// Passes of several plans (any lengths, with the runtime-length stages) in
+// one launch: job j owns blocks first_block .. first_block + nblocks - 1 and
+// runs its pass with them as its own grid.
+template <typename T, int SIGN>
+__global__ void __launch_bounds__(NT, MINB) fft_pass_group_kernel(const __grid_constant__ dmg_fft_group g) {
+  int j = 0;
+  while (j + 1 < g.count && (int64_t)blockIdx.x >= g.job[j + 1].first_block) ++j;
+  const dmg_fft_group_job &job = g.job[j];
+  pass_body<T, SIGN, 0, false>(job.p, job.bt, (int64_t)blockIdx.x - job.first_block, job.nblocks);
+}
+
+// One grouped launch: every job gets blocks in proportion to its tiles (at
+// least one, at most its tile count) out of the blocks that fill the SMs at
+// the largest job's shared memory.
+template <typename T, int SIGN>
+int launch_group(dmg_fft_group g, cudaStream_t s) {
+  size_t smem = 0;
+  int64_t tiles = 0;
+  for (int j = 0; j < g.count; ++j) {
+    const size_t sj = smem_layout<T>(g.job[j].p, false).total;
+    smem = sj > smem ? sj : smem;
+    tiles += g.job[j].p.ntiles * g.job[j].bt.count;
+  }
+  auto k = fft_pass_group_kernel<T, SIGN>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return dmg_error(DMG_ERR_CUDA, "grouped fft pass smem %zu: %s", smem, cudaGetErrorString(e));
+  }
+  int dev = 0, nsm = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, NT, smem);
+  if (per_sm < 1) return dmg_error(DMG_ERR_UNSUPPORTED, "grouped fft pass does not fit on an SM (smem %zu)", smem);
+  const int64_t budget = (int64_t)nsm * per_sm;
+  int64_t first = 0;
+  for (int j = 0; j < g.count; ++j) {
+    const int64_t tj = g.job[j].p.ntiles * g.job[j].bt.count;
+    int64_t nb = tiles > 0 ? (budget * tj + tiles - 1) / tiles : 1;
+    if (nb > tj) nb = tj;
+    if (nb < 1) nb = 1;
+    g.job[j].first_block = first;
+    g.job[j].nblocks = nb;
+    first += nb;
+  }
+  k<<<(unsigned)first, NT, smem, s>>>(g);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return dmg_error(DMG_ERR_CUDA, "grouped fft pass launch: %s", cudaGetErrorString(e));
+  return DMG_OK;
 }
 
 template <typename T, int SIGN, int NF, bool TC = false>

@@ -193,6 +193,19 @@ int dmg_split_run_batch(SplitPlan plan, int direction, void *stream, int count, 
 long long dmg_split_extent64(SplitPlan plan);
 /** Kernel launches of one dmg_split_run_batch call. */
 int dmg_split_batch_launches(SplitPlan plan, int direction, int count);
+/** Most plans in one dmg_split_run_group call. */
+#define DMG_SPLIT_MAXGROUP 16
+/** runSplitPlan on up to DMG_SPLIT_MAXGROUP different plans (any sizes,
+ * decompositions and pass counts; no counterpart in the reference), each on
+ * its own dat and workspace: the k-th passes of all plans share one launch,
+ * so a group of small transforms takes as many pass launches as its longest
+ * plan has passes.  Every plan must have a runtime radix schedule
+ * (DMG_RADIX_PLAN8 or DMG_RADIX_PLAN4) and the same arithmetic; the results
+ * are the bits of runSplitPlan on each plan.  Buffers of different plans
+ * must not overlap. */
+int dmg_split_run_group(int count, SplitPlan const *plans, int direction, void *stream);
+/** Kernel launches of one dmg_split_run_group call (0 if the group is invalid). */
+int dmg_split_group_launches(int count, SplitPlan const *plans, int direction);
 /** Select the pass schedule (no counterpart in the reference). */
 int dmg_split_set_schedule(SplitPlan plan, int schedule);
 /** The schedule in use: DMG_SCHEDULE_LINES or DMG_SCHEDULE_SPLIT. */
