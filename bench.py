@@ -672,10 +672,13 @@ def serve_study(args, njobs):
     classes = sorted(set(zip(sides.tolist(), dtypes.tolist())))
     flops = float(sum(2 * flops_per_transform(int(sd) ** 3) for sd in sides))
 
-    def make_server(slots, batch):
-        return api.Server(grid, args.arena_gb << 30, slots=slots, max_batch=batch)
+    def make_server(slots, batch, mix=0):
+        srv = api.Server(grid, args.arena_gb << 30, slots=slots, max_batch=batch)
+        if mix:
+            srv.set_mixing(mix)
+        return srv
 
-    srv = make_server(args.slots, args.batch)
+    srv = make_server(args.slots, args.batch, args.mix_side)
     # one input per class (uniform[-1,1)), pinned spectrum / output arrays per class: jobs of a class carry
     # the same values, so concurrent jobs of a class write identical results into them
     bufs = {}
@@ -772,7 +775,8 @@ def serve_study(args, njobs):
                    "gflops": round(flops / span / 1e9, 2), "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 3),
                    "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 3),
                    "mean_batch": round(float(batches.mean()), 2), "max_batch": int(batches.max()),
-                   "slots": args.slots, "max_batch_limit": args.batch, "arena_gib": args.arena_gb},
+                   "slots": args.slots, "max_batch_limit": args.batch, "arena_gib": args.arena_gb,
+                   "mixing_max_side": args.mix_side},
         "arithmetic": "served: complex128 in double-float, complex64 in FP32 (sides up to 512 have no 1024-point "
                       "lines for the tensor-core stages)",
         "alone": alone_same,
@@ -1039,6 +1043,72 @@ def run_group(args):
     print(json.dumps(group_study(max(args.steps, 10))))
 
 
+def compare_study(n=256, ranks=64, trials=10, repeat=10):
+    """Slab plan against the autotuned plan, the comparison of plan_compare.c:319-358: an n^3 complex128 cube
+    (uniform[-1,1), seed 4) in the block decomposition on makeProcessorGrid's grid for `ranks` virtual ranks;
+    the slab plan is makeParallelPlan with B = [1, n, n], the other autotuneParallelPlan (workspace 2 x 4 x the
+    start extent per rank, the reference's FUDGE).  Each plan: `trials` trials of `repeat` forward transforms
+    (CUDA events), best and worst trial, in double-float (the arithmetic the autotuner times) and in native
+    FP64."""
+    import torch
+
+    from decomp_mpi_gb300 import api
+
+    dev = torch.device("cuda:0")
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    comm = api.Comm(ranks)
+    grid = api.processor_grid(comm, [n, n, n])
+    start = api.decomp_from_spec(comm, "packed:block(%d,%d)|block(%d,%d)|block(%d,%d)" % (
+        n, grid[0], n, grid[1], n, grid[2]))
+    ext = start.extent()
+    length = 2 * 4 * ext
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(4)
+    dat = torch.empty(ranks * ext, dtype=torch.complex128, device=dev)
+    dat.real.uniform_(-1, 1, generator=gen)
+    dat.imag.uniform_(-1, 1, generator=gen)
+    keep = dat.clone()
+    work = torch.zeros(ranks * length, dtype=torch.complex128, device=dev)
+    slab = api.SplitPlan(start, dat.data_ptr(), length, work.data_ptr(), B=[1, n, n])
+    t0 = time.monotonic()
+    api.autotune_cache_clear()
+    auto = api.SplitPlan(start, dat.data_ptr(), length, work.data_ptr(), autotune=True)
+    tune_s = time.monotonic() - t0
+    dat.copy_(keep)  # the autotuner ran transforms on the caller's arrays
+    out = {"metric": "slab vs autotuned split plan: forward transform ms (best / worst of %d trials of %d)" % (
+        trials, repeat), "n": n, "virtual_ranks": ranks, "start_grid": grid, "autotune_s": round(tune_s, 3),
+        "autotune_timed_configs": api.autotune_last_timed()}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for ar, name in ((api.ARITH_DF, "double_float"), (api.ARITH_FP64, "fp64")):
+        res = {}
+        for label, sp in (("slab", slab), ("auto", auto)):
+            sp.set_arith(ar)
+            for _ in range(3):
+                sp.run(api.FFTW_FORWARD, sh)
+            torch.cuda.synchronize()
+            per = []
+            for _ in range(trials):
+                e0.record(stream)
+                for _ in range(repeat):
+                    sp.run(api.FFTW_FORWARD, sh)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                per.append(e0.elapsed_time(e1) / repeat)
+            res[label] = {"A": sp.A_factors, "schedule": "lines" if sp.schedule == api.SCHEDULE_LINES else "split",
+                          "best_ms": round(min(per), 4), "worst_ms": round(max(per), 4),
+                          "gflops_best": round(flops_per_transform(n ** 3) / (min(per) * 1e-3) / 1e9, 1)}
+        res["slab_over_auto_best"] = round(res["slab"]["best_ms"] / res["auto"]["best_ms"], 3)
+        out[name] = res
+    slab.free()
+    auto.free()
+    return out
+
+
+def run_compare(args):
+    print(json.dumps(compare_study(args.n if args.n != N_SIDE else 256, args.grid * args.grid)))
+
+
 def run_fft(args):
     """Split FFT alone: forward and inverse timings (CUDA events, median of 5 after 2 warm-up runs) and per-pass
     times at n^3 on a g x g grid (--grid, 8 by default) in the factor_reverse decomposition of the headline chain
@@ -1167,11 +1237,15 @@ def main():
     ap.add_argument("--serve", action="store_true", help="served form: Poisson stream of mixed-size jobs")
     ap.add_argument("--precision", action="store_true", help="precision form: 1024^3 complex64 with error")
     ap.add_argument("--group", action="store_true", help="grouped form: 16 uneven small transforms per launch")
+    ap.add_argument("--compare", action="store_true",
+                    help="slab plan vs autotuned plan at --n (256 by default) on --grid^2 virtual ranks")
     ap.add_argument("--jobs", type=int, default=200, help="with --serve: jobs in the stream")
     ap.add_argument("--rate", type=float, default=2000.0, help="with --serve: mean arrivals per second")
     ap.add_argument("--slots", type=int, default=4, help="with --serve: stream slots")
     ap.add_argument("--batch", type=int, default=8, help="with --serve: jobs that may share launches")
     ap.add_argument("--arena-gb", dest="arena_gb", type=int, default=96, help="with --serve: device arena")
+    ap.add_argument("--mix-side", dest="mix_side", type=int, default=0,
+                    help="with --serve: jobs of sides up to this share launches with other sides (0: off)")
     ap.add_argument("--no-extras", dest="no_extras", action="store_true",
                     help="default run: leave out the reshape-sweep subset and the served stream")
     args = ap.parse_args()
@@ -1179,7 +1253,7 @@ def main():
     if args.impl == "reference":
         run_reference(args)
         return
-    if not (args.sweep or args.fft or args.serve or args.precision or args.group):
+    if not (args.sweep or args.fft or args.serve or args.precision or args.group or args.compare):
         run_gpu(args)  # every rank: one replica of the workload per GPU
         return
     if int(os.environ.get("WORLD_SIZE", "1")) > 1 and int(os.environ.get("RANK", "0")) != 0:
@@ -1198,6 +1272,9 @@ def main():
         return
     if args.group:
         run_group(args)
+        return
+    if args.compare:
+        run_compare(args)
         return
 
 

@@ -120,12 +120,14 @@ SIGNATURES = {
     "dmg_split_run_batch": (_i, [_vp, _i, _vp, _i, _vp, _vp, _vp]),
     "dmg_split_batch_launches": (_i, [_vp, _i, _i]),
     "dmg_split_run_group": (_i, [_i, _vp, _i, _vp]),
+    "dmg_split_run_group_batch": (_i, [_i, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
     "dmg_split_group_launches": (_i, [_i, _vp, _i]),
     "dmg_split_extent64": (_ll, [_vp]),
     "dmg_decomp_scale": (_i, [_vp, _i, _vp, ctypes.POINTER(_vp), _i, _vp]),
     "dmg_visit_fill_index": (_i, [_vp, _i, _vp, _vp]),
     "dmg_server_create": (_vp, [_i, _ll, _i, _i]),
     "dmg_server_set_arith": (_i, [_vp, _i, _i]),
+    "dmg_server_set_mixing": (_i, [_vp, _i]),
     "dmg_server_job_sizes": (_i, [_vp, _i, _i, ctypes.POINTER(_ll), ctypes.POINTER(_ll), ctypes.POINTER(_ll)]),
     "dmg_server_submit": (_ll, [_vp, _vp]),
     "dmg_server_poll": (_i, [_vp, _vp, _i]),

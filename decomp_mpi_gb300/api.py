@@ -535,6 +535,19 @@ def split_run_group(plans, direction, stream=None):
     check(load().dmg_split_run_group(n, P, int(direction), ctypes.c_void_p(stream or 0)), "dmg_split_run_group")
 
 
+def split_run_group_batch(plans, njobs, dats, works, scales, direction, stream=None):
+    """dmg_split_run_group_batch: plan i transforms njobs[i] arrays; dats / works / scales list them plan by plan
+    (scales: device int words, for double-float plans)."""
+    n, m = len(plans), len(dats)
+    P = (ctypes.c_void_p * n)(*[p.h for p in plans])
+    J = (ctypes.c_int * n)(*[int(x) for x in njobs])
+    D = (ctypes.c_void_p * m)(*[ctypes.c_void_p(x) for x in dats])
+    W = (ctypes.c_void_p * m)(*[ctypes.c_void_p(x) for x in works])
+    S = (ctypes.c_void_p * m)(*[ctypes.c_void_p(x) for x in (scales or [0] * m)])
+    check(load().dmg_split_run_group_batch(n, P, J, D, W, S, int(direction), ctypes.c_void_p(stream or 0)),
+          "dmg_split_run_group_batch")
+
+
 def split_group_launches(plans, direction) -> int:
     n = len(plans)
     P = (ctypes.c_void_p * n)(*[p.h for p in plans])
@@ -684,6 +697,10 @@ class Server:
         """Arithmetic of the server's plans of one element type (C128: ARITH_DF or ARITH_FP64; C64: ARITH_FP32 or
         ARITH_TC16); call it while no job is queued or running."""
         check(self.lib.dmg_server_set_arith(self.h, int(dtype), int(arith)), "dmg_server_set_arith")
+
+    def set_mixing(self, max_side):
+        """Jobs of sides up to max_side may share launches with other sides (0: only one side per batch)."""
+        check(self.lib.dmg_server_set_mixing(self.h, int(max_side)), "dmg_server_set_mixing")
 
     def sizes(self, side, dtype):
         """Element counts of a job's host arrays: (input, spectrum, output)."""

@@ -6,11 +6,16 @@
  * and (2) fills every idle stream slot with the oldest queued job that fits
  * the arena (a few younger jobs may pass a head that does not fit yet)
  * plus the queued jobs of the same side and type that also fit, up to the
- * batch limit.  A batch runs on its slot's stream: per job the host-to-
- * device copy and the block -> rotate reshape, then the forward split FFT
- * of all jobs as shared launches, the spectrum copies, the inverse as
- * shared launches and the output copies, and an event.  Plans and their
- * device tables are cached per (side, type).
+ * batch limit; with mixing on, queued jobs of other sides up to the mixing
+ * limit (and the same type) join a head of such a side too.  A batch runs
+ * on its slot's stream: per job the host-to-device copy, the block -> rotate
+ * reshapes of all jobs in shared launches, then the forward split FFT of all
+ * jobs as shared launches (one launch per pass for jobs of one side; the
+ * k-th passes of every side in one launch for a mixed batch), the spectrum
+ * copies, the inverse as shared launches and the output copies, and an
+ * event.  Plans and their device tables are cached per (side, type); the
+ * plans of sides that may mix run the runtime radix schedule PLAN8, which
+ * the grouped pass launch needs.
  */
 #define _POSIX_C_SOURCE 200809L
 #include <pthread.h>
@@ -66,6 +71,7 @@ typedef struct {
 struct dmg_server {
   int grid, P, nslots, max_batch, dev;
   int arith[2]; /* arithmetic of complex128 and complex64 plans (DMG_ARITH_*; -1: the plan's default) */
+  int mix_side; /* jobs of sides up to this may share launches with other sides (0: none) */
   MPI_Comm comm;
   char *base;
   arena ar;
@@ -136,6 +142,7 @@ static plan_entry *plan_make(struct dmg_server *s, int side, int dtype) {
   if (s->arith[dtype == DMG_C128 ? 0 : 1] >= 0 &&
       dmg_split_set_arith(pe->sp, s->arith[dtype == DMG_C128 ? 0 : 1]) != DMG_OK)
     goto fail;
+  if (side <= s->mix_side && dmg_split_set_radix(pe->sp, DMG_RADIX_PLAN8) != DMG_OK) goto fail;
   pe->bytes_in = (long long)s->P * pe->pitch_blk * pe->es;
   pe->bytes_dat = (long long)s->P * pe->pitch_rot * pe->es;
   pe->bytes_work = (long long)s->P * pe->len * pe->es;
@@ -213,38 +220,55 @@ static void push_done(struct dmg_server *s, job_rec *jr) {
   s->done[s->ndone++] = jr;
 }
 
-/* Enqueue a batch on a slot's stream. */
+/* Enqueue a batch on a slot's stream.  The slot's jobs are in plan order
+ * (the jobs of one plan next to each other). */
 static int launch_batch(struct dmg_server *s, slot *sl) {
   job_rec **jobs = sl->jobs;
   const int k = sl->njobs;
-  const plan_entry *pe = jobs[0]->pe;
   void *st = sl->stream;
   void *dats[DMG_FFT_MAXBATCH], *works[DMG_FFT_MAXBATCH];
   int *scales[DMG_FFT_MAXBATCH];
   int rc = DMG_OK;
   ReshapePlan plans[DMG_FFT_MAXBATCH];
   const void *ins[DMG_FFT_MAXBATCH];
+  SplitPlan splits[DMG_FFT_MAXBATCH];
+  int njobs[DMG_FFT_MAXBATCH], nplans = 0;
   for (int i = 0; i < k && rc == DMG_OK; ++i) {
+    const plan_entry *pe = jobs[i]->pe;
     char *in = s->base + jobs[i]->off_in;
     dats[i] = s->base + jobs[i]->off_dat;
     works[i] = s->base + jobs[i]->off_work;
     scales[i] = (int *)(s->base + jobs[i]->off_scale);
     plans[i] = pe->r01;
     ins[i] = in;
+    if (i == 0 || pe != jobs[i - 1]->pe) {
+      splits[nplans] = pe->sp;
+      njobs[nplans++] = 0;
+    }
+    njobs[nplans - 1]++;
     rc = dmg_rt_copy_async(in, jobs[i]->j.input, (size_t)pe->bytes_in, 0, st);
   }
-  /* every job's block -> rotate reshape in one launch */
+  /* every job's block -> rotate reshape in shared launches */
   if (rc == DMG_OK) rc = dmg_reshape_run_group(k, plans, ins, dats, st);
-  if (rc == DMG_OK) rc = dmg_split_run_batch(pe->sp, FFTW_FORWARD, st, k, dats, works, scales);
-  for (int i = 0; i < k && rc == DMG_OK; ++i)
-    if (jobs[i]->j.spectrum)
-      rc = dmg_rt_copy2d_async(jobs[i]->j.spectrum, (size_t)(pe->ext * pe->es), works[i], (size_t)(pe->len * pe->es),
-                               (size_t)(pe->ext * pe->es), (size_t)s->P, 1, st);
-  if (rc == DMG_OK) rc = dmg_split_run_batch(pe->sp, FFTW_BACKWARD, st, k, dats, works, scales);
-  for (int i = 0; i < k && rc == DMG_OK; ++i)
-    if (jobs[i]->j.output) rc = dmg_rt_copy_async(jobs[i]->j.output, dats[i], (size_t)pe->bytes_dat, 1, st);
+  for (int dir = 0; dir < 2 && rc == DMG_OK; ++dir) {
+    const int direction = dir == 0 ? FFTW_FORWARD : FFTW_BACKWARD;
+    rc = nplans == 1 ? dmg_split_run_batch(splits[0], direction, st, k, dats, works, scales)
+                     : dmg_split_run_group_batch(nplans, splits, njobs, dats, works, scales, direction, st);
+    for (int i = 0; i < k && rc == DMG_OK; ++i) {
+      const plan_entry *pe = jobs[i]->pe;
+      if (dir == 0 && jobs[i]->j.spectrum)
+        rc = dmg_rt_copy2d_async(jobs[i]->j.spectrum, (size_t)(pe->ext * pe->es), works[i],
+                                 (size_t)(pe->len * pe->es), (size_t)(pe->ext * pe->es), (size_t)s->P, 1, st);
+      if (dir == 1 && jobs[i]->j.output)
+        rc = dmg_rt_copy_async(jobs[i]->j.output, dats[i], (size_t)pe->bytes_dat, 1, st);
+    }
+  }
   int rr = dmg_rt_event_record(sl->event, st);
   return rc != DMG_OK ? rc : rr;
+}
+
+static int mixes(const struct dmg_server *s, const plan_entry *a, const plan_entry *b) {
+  return a == b || (a->dtype == b->dtype && a->side <= s->mix_side && b->side <= s->mix_side);
 }
 
 /* Fill idle slots; returns how many batches started. */
@@ -268,18 +292,28 @@ static int admit(struct dmg_server *s) {
     q_remove(s, head_prev, head);
     sl->njobs = 0;
     sl->jobs[sl->njobs++] = head;
-    /* queued jobs of the same plan that also fit join the batch */
+    /* queued jobs of the same plan (or, with mixing, of another side that
+     * may mix) that also fit join the batch */
     prev = NULL;
     jr = s->q_head;
     while (jr && sl->njobs < s->max_batch) {
       job_rec *nx = jr->next;
-      if (jr->pe == head->pe && job_alloc(s, jr)) {
+      if (mixes(s, head->pe, jr->pe) && job_alloc(s, jr)) {
         q_remove(s, prev, jr);
         sl->jobs[sl->njobs++] = jr;
       } else {
         prev = jr;
       }
       jr = nx;
+    }
+    /* plan order: each plan's jobs next to each other, plans in order of first arrival */
+    for (int i = 1; i < sl->njobs; ++i) {
+      int last = i - 1;
+      while (last >= 0 && sl->jobs[last]->pe != sl->jobs[i]->pe) --last;
+      if (last < 0 || last == i - 1) continue;
+      job_rec *t = sl->jobs[i];
+      memmove(&sl->jobs[last + 2], &sl->jobs[last + 1], (size_t)(i - last - 1) * sizeof(job_rec *));
+      sl->jobs[last + 1] = t;
     }
     const double t = now_s();
     for (int i = 0; i < sl->njobs; ++i) {
@@ -402,6 +436,21 @@ int dmg_server_set_arith(DmgServer s, int dtype, int arith) {
     s->arith[dtype == DMG_C128 ? 0 : 1] = arith;
     for (int i = 0; i < s->nplans && st == DMG_OK; ++i)
       if (s->plans[i]->dtype == dtype) st = dmg_split_set_arith(s->plans[i]->sp, arith);
+  }
+  pthread_mutex_unlock(&s->mu);
+  return st;
+}
+
+int dmg_server_set_mixing(DmgServer s, int max_side) {
+  if (!s || max_side < 0) return dmg_error(DMG_ERR_ARG, "dmg_server_set_mixing: server %p, side %d", (void *)s, max_side);
+  pthread_mutex_lock(&s->mu);
+  int st = DMG_OK;
+  if (s->running || s->nqueued) {
+    st = dmg_error(DMG_ERR_ARG, "dmg_server_set_mixing: jobs are queued or running; drain the server first");
+  } else {
+    s->mix_side = max_side;
+    for (int i = 0; i < s->nplans && st == DMG_OK; ++i)
+      st = dmg_split_set_radix(s->plans[i]->sp, s->plans[i]->side <= max_side ? DMG_RADIX_PLAN8 : DMG_RADIX_FIXED);
   }
   pthread_mutex_unlock(&s->mu);
   return st;

@@ -1324,8 +1324,9 @@ _Static_assert(DMG_SPLIT_MAXGROUP == DMG_FFT_MAXGROUP, "a group is one launch pe
  * in the launch before, on the same stream.  Every plan runs its passes with
  * the runtime stages of its radix schedule, so it must have one
  * (DMG_RADIX_PLAN8 or DMG_RADIX_PLAN4); its results are then the bits of
- * dmg_split_run on the same plan. */
-static int group_check(int count, SplitPlan const *plans, int direction, const char *who) {
+ * dmg_split_run on the same plan.  own_buffers: the plans' dat and workspace
+ * are the arrays (else the caller lists them). */
+static int group_check(int count, SplitPlan const *plans, int direction, int own_buffers, const char *who) {
   if (direction != FFTW_FORWARD && direction != FFTW_BACKWARD)
     return dmg_error(DMG_ERR_ARG, "%s: direction %d", who, direction);
   if (count < 1 || count > DMG_FFT_MAXGROUP)
@@ -1333,7 +1334,7 @@ static int group_check(int count, SplitPlan const *plans, int direction, const c
   for (int i = 0; i < count; ++i) {
     if (!plans[i]) return dmg_error(DMG_ERR_ARG, "%s: NULL plan %d", who, i);
     const struct dmg_split_impl *im = plans[i]->impl;
-    if (!im->dat || !im->work) return dmg_error(DMG_ERR_ARG, "%s: NULL buffer in plan %d", who, i);
+    if (own_buffers && (!im->dat || !im->work)) return dmg_error(DMG_ERR_ARG, "%s: NULL buffer in plan %d", who, i);
     if (im->radix == DMG_RADIX_FIXED)
       return dmg_error(DMG_ERR_ARG, "%s: plan %d has the fixed radix schedules; set DMG_RADIX_PLAN8 or "
                                     "DMG_RADIX_PLAN4 on every plan of a group", who, i);
@@ -1346,40 +1347,58 @@ static int group_check(int count, SplitPlan const *plans, int direction, const c
   return DMG_OK;
 }
 
-int dmg_split_run_group(int count, SplitPlan const *plans, int direction, void *stream) {
-  if (!plans) return dmg_error(DMG_ERR_ARG, "dmg_split_run_group: NULL plan list");
-  int st = group_check(count, plans, direction, "dmg_split_run_group");
-  if (st != DMG_OK) return st;
-  int most = 0;
-  for (int i = 0; i < count; ++i) {
+/* The run over a checked group: plan i transforms njobs[i] arrays, listed
+ * plan by plan in dats / works / scales (njobs NULL: one array per plan, the
+ * plan's own dat and workspace, with its own exponent word). */
+static int group_run(int count, SplitPlan const *plans, const int *njobs, void *const *dats, void *const *works,
+                     int *const *scales, int direction, void *stream) {
+  int st = DMG_OK, most = 0;
+  int32_t L[DMG_FFT_MAXDIM], A[DMG_FFT_MAXDIM];
+  for (int i = 0, at = 0; i < count; ++i) {
     struct dmg_split_impl *im = plans[i]->impl;
     if (!im->dev_valid && (st = impl_upload(im)) != DMG_OK) return st;
     const int cnt = direction == FFTW_FORWARD ? im->nfwd : im->ninv;
     if (cnt > most) most = cnt;
+    const int nj = njobs ? njobs[i] : 1;
     if (im->arith == DMG_ARITH_DF) {
       const pass_rec *first = direction == FFTW_FORWARD ? &im->fwd[0] : &im->inv[0];
-      st = launch_maxexp(im, first, first->in_buf == BUF_DAT ? im->dat : im->work, stream);
+      for (int d = 0; d < DMG_FFT_MAXDIM; ++d) {
+        L[d] = im->L[d];
+        A[d] = im->A[d];
+      }
+      for (int j = 0; j < nj && st == DMG_OK; ++j) {
+        const void *src = first->in_buf == BUF_DAT ? (njobs ? dats[at + j] : im->dat)
+                                                   : (njobs ? works[at + j] : im->work);
+        st = dmg_fft_maxexp_launch(&first->p.in, im->ndim, A, L, src, njobs ? scales[at + j] : im->d_scale, stream);
+      }
       if (st != DMG_OK) return st;
     }
+    at += nj;
   }
   /* the group's descriptor is about 16 KB: keep it off the stack */
   struct dmg_fft_group *g = (struct dmg_fft_group *)calloc(1, sizeof(struct dmg_fft_group));
-  if (!g) return dmg_error(DMG_ERR_NOMEM, "dmg_split_run_group: out of memory");
+  if (!g) return dmg_error(DMG_ERR_NOMEM, "split group: out of memory");
   const int dt = arith_dtype(plans[0]->impl);
   for (int k = 0; k < most && st == DMG_OK; ++k) {
     g->count = 0;
-    for (int i = 0; i < count; ++i) {
+    for (int i = 0, at = 0; i < count; ++i) {
       struct dmg_split_impl *im = plans[i]->impl;
       const int cnt = direction == FFTW_FORWARD ? im->nfwd : im->ninv;
-      if (k >= cnt) continue;
-      const pass_rec *r = direction == FFTW_FORWARD ? &im->fwd[k] : &im->inv[k];
-      struct dmg_fft_group_job *job = &g->job[g->count++];
-      memset(job, 0, sizeof(*job));
-      job->p = r->p;
-      job->bt.count = 1;
-      job->bt.src[0] = r->in_buf == BUF_DAT ? im->dat : im->work;
-      job->bt.dst[0] = r->out_buf == BUF_DAT ? im->dat : im->work;
-      job->bt.scale_exp[0] = r->p.scale_exp;
+      const int nj = njobs ? njobs[i] : 1;
+      if (k < cnt) {
+        const pass_rec *r = direction == FFTW_FORWARD ? &im->fwd[k] : &im->inv[k];
+        struct dmg_fft_group_job *job = &g->job[g->count++];
+        memset(job, 0, sizeof(*job));
+        job->p = r->p;
+        job->bt.count = nj;
+        for (int j = 0; j < nj; ++j) {
+          void *dat = njobs ? dats[at + j] : im->dat, *work = njobs ? works[at + j] : im->work;
+          job->bt.src[j] = r->in_buf == BUF_DAT ? dat : work;
+          job->bt.dst[j] = r->out_buf == BUF_DAT ? dat : work;
+          job->bt.scale_exp[j] = njobs ? scales[at + j] : r->p.scale_exp;
+        }
+      }
+      at += nj;
     }
     st = dmg_fft_pass_launch_group(g, dt, stream);
   }
@@ -1387,8 +1406,32 @@ int dmg_split_run_group(int count, SplitPlan const *plans, int direction, void *
   return st;
 }
 
+int dmg_split_run_group(int count, SplitPlan const *plans, int direction, void *stream) {
+  if (!plans) return dmg_error(DMG_ERR_ARG, "dmg_split_run_group: NULL plan list");
+  int st = group_check(count, plans, direction, 1, "dmg_split_run_group");
+  if (st != DMG_OK) return st;
+  return group_run(count, plans, NULL, NULL, NULL, NULL, direction, stream);
+}
+
+int dmg_split_run_group_batch(int count, SplitPlan const *plans, const int *njobs, void *const *dats,
+                              void *const *works, int *const *scales, int direction, void *stream) {
+  if (!plans || !njobs || !dats || !works) return dmg_error(DMG_ERR_ARG, "dmg_split_run_group_batch: NULL list");
+  int st = group_check(count, plans, direction, 0, "dmg_split_run_group_batch");
+  if (st != DMG_OK) return st;
+  for (int i = 0, at = 0; i < count; ++i) {
+    if (njobs[i] < 1 || njobs[i] > DMG_FFT_MAXBATCH)
+      return dmg_error(DMG_ERR_ARG, "dmg_split_run_group_batch: plan %d with %d arrays (1 to %d)", i, njobs[i],
+                       DMG_FFT_MAXBATCH);
+    for (int j = at; j < at + njobs[i]; ++j)
+      if (!dats[j] || !works[j] || (plans[i]->impl->arith == DMG_ARITH_DF && (!scales || !scales[j])))
+        return dmg_error(DMG_ERR_ARG, "dmg_split_run_group_batch: NULL buffer for array %d", j);
+    at += njobs[i];
+  }
+  return group_run(count, plans, njobs, dats, works, scales, direction, stream);
+}
+
 int dmg_split_group_launches(int count, SplitPlan const *plans, int direction) {
-  if (!plans || group_check(count, plans, direction, "dmg_split_group_launches") != DMG_OK) return 0;
+  if (!plans || group_check(count, plans, direction, 1, "dmg_split_group_launches") != DMG_OK) return 0;
   int most = 0, pre = 0;
   for (int i = 0; i < count; ++i) {
     const struct dmg_split_impl *im = plans[i]->impl;

@@ -57,6 +57,13 @@ DmgServer dmg_server_create(int grid, long long arena_bytes, int slots, int max_
  * DMG_ARITH_TC16 for DMG_C64.  Applies to cached plans too; refused while
  * jobs are queued or running. */
 int dmg_server_set_arith(DmgServer s, int dtype, int arith);
+/** Mixing: jobs of sides up to max_side (and one element type) may share
+ * launches with jobs of other such sides, the reshapes and every split-FFT
+ * pass of a mixed batch in one launch each; the plans of those sides run the
+ * runtime radix schedule DMG_RADIX_PLAN8.  0 (the default) batches only jobs
+ * of one side.  Applies to cached plans too; refused while jobs are queued
+ * or running. */
+int dmg_server_set_mixing(DmgServer s, int max_side);
 /** Element counts of a job's host arrays (input, spectrum, output). */
 int dmg_server_job_sizes(DmgServer s, int side, int dtype, long long *input, long long *spectrum, long long *output);
 /** Queue a job; returns its id (>= 0) or a negative error code.  A job that

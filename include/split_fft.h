@@ -204,6 +204,12 @@ int dmg_split_batch_launches(SplitPlan plan, int direction, int count);
  * are the bits of runSplitPlan on each plan.  Buffers of different plans
  * must not overlap. */
 int dmg_split_run_group(int count, SplitPlan const *plans, int direction, void *stream);
+/** The same as a job table: plan i transforms njobs[i] (1 to 16) arrays of
+ * its shape, as dmg_split_run_batch does for one plan; dats, works and
+ * scales (device int words, for double-float plans) list the arrays plan by
+ * plan.  The plans' own dat and workspace are not used. */
+int dmg_split_run_group_batch(int count, SplitPlan const *plans, const int *njobs, void *const *dats,
+                              void *const *works, int *const *scales, int direction, void *stream);
 /** Kernel launches of one dmg_split_run_group call (0 if the group is invalid). */
 int dmg_split_group_launches(int count, SplitPlan const *plans, int direction);
 /** Select the pass schedule (no counterpart in the reference). */

@@ -225,3 +225,47 @@ def test_server_arithmetic_choice(cuda):
         e_spec, e_back = _check_job(srv, side, dtype, g, hs, ho)
         assert e_spec < TOL[dtype] and e_back < TOL[dtype], (side, dtype, e_spec, e_back)
     srv.close()
+
+
+@pytest.mark.parametrize("arith128", [None, api.ARITH_FP64], ids=["df", "fp64"])
+def test_mixed_sides_share_launches(arith128, cuda):
+    """dmg_server_set_mixing: jobs of different sides (one element type per batch) share the reshape and pass
+    launches.  Each job's spectrum and inverse are the same bits as on a one-slot server that runs it alone
+    with the same plans, and match the FP64 oracle; some batch holds more jobs than any one (side, type)
+    class has, so it mixed sides; the setting is refused while jobs are queued."""
+    jobs = _job_list() + [(40, api.C128, 300), (40, api.C64, 301), (60, api.C128, 302)]
+    classes = {}
+    for side, dtype, _ in jobs:
+        classes[(side, dtype)] = classes.get((side, dtype), 0) + 1
+    alone = api.Server(GRID, 1 << 30, slots=1, max_batch=1)
+    alone.set_mixing(64)
+    if arith128 is not None:
+        alone.set_arith(api.C128, arith128)
+    a_bufs, _ = _run(alone, jobs, cuda, one_at_a_time=True)
+    alone.close()
+    mix = api.Server(GRID, 1 << 30, slots=1, max_batch=16)
+    mix.set_mixing(64)
+    if arith128 is not None:
+        mix.set_arith(api.C128, arith128)
+    m_bufs, m_done = _run(mix, jobs, cuda, one_at_a_time=False)
+    assert max(d["batch"] for d in m_done) > max(classes.values())
+    srv = api.Server(GRID, 1 << 26, slots=1, max_batch=1)
+    for (side, dtype, seed), a, m in zip(jobs, a_bufs, m_bufs):
+        spec_held, out_held = _held(srv, side, dtype)
+        assert np.array_equal(a[1].numpy()[spec_held], m[1].numpy()[spec_held]), (side, dtype)
+        assert np.array_equal(a[2].numpy()[out_held], m[2].numpy()[out_held]), (side, dtype)
+        g = _cube(side, dtype, seed).astype(np.complex128)
+        e_spec, e_back = _check_job(srv, side, dtype, g, m[1], m[2])
+        assert e_spec < TOL[dtype] and e_back < TOL[dtype], (side, dtype, e_spec, e_back)
+    srv.close()
+    import torch
+    n_in, _, _ = mix.sizes(24, api.C128)
+    x = torch.zeros(n_in, dtype=torch.complex128).pin_memory()
+    for _ in range(4):
+        mix.submit(24, api.C128, x.data_ptr())
+    with pytest.raises(Exception):
+        mix.set_mixing(0)
+    mix.drain()
+    mix.poll()
+    mix.set_mixing(0)
+    mix.close()

@@ -160,3 +160,30 @@ def test_group_of_one_and_of_sixteen(cuda):
         torch.cuda.synchronize()
         for i, j in enumerate(jobs):
             assert np.array_equal(_bits(j.work), _bits(want[i])), (len(sel), i)
+
+
+@pytest.mark.gpu
+def test_group_batch_job_table(cuda):
+    """dmg_split_run_group_batch: two plans of different shapes with two and one arrays each give the bits of
+    each array's own run (double-float, with an exponent word per array)."""
+    import torch
+    stream = torch.cuda.current_stream(cuda).cuda_stream
+    specs = [GROUP[0], GROUP[2]]
+    jobs = [[_Job(P, spec, shape, sch, api.C128, api.ARITH_DF, api.RADIX_PLAN8, 60 + 10 * i + k, cuda)
+             for k in range(2 - i)] for i, (P, spec, shape, sch) in enumerate(specs)]
+    want = []
+    for arrs in jobs:
+        for j in arrs:
+            j.plan.run(api.FFTW_FORWARD, stream)
+            torch.cuda.synchronize()
+            want.append(j.work.clone())
+            j.reset()
+    torch.cuda.synchronize()
+    flat = [j for arrs in jobs for j in arrs]
+    scales = torch.zeros(64 * len(flat), dtype=torch.int32, device=cuda)
+    api.split_run_group_batch([arrs[0].plan for arrs in jobs], [len(a) for a in jobs],
+                              [j.dat.data_ptr() for j in flat], [j.work.data_ptr() for j in flat],
+                              [scales.data_ptr() + 256 * i for i in range(len(flat))], api.FFTW_FORWARD, stream)
+    torch.cuda.synchronize()
+    for i, j in enumerate(flat):
+        assert np.array_equal(_bits(j.work), _bits(want[i])), i
