@@ -420,6 +420,8 @@ def run_gpu(args):
         torch.cuda.empty_cache()
         extras["grouped_small"] = group_study()
         torch.cuda.empty_cache()
+        extras["plan_compare"] = compare_study(256, 64)
+        torch.cuda.empty_cache()
     cpu = cpu_baseline(args, reps=3)
     line = {
         "metric": "3D FFT GFLOP/s (5 N log2 N per transform) + reshape GB/s",
@@ -667,7 +669,9 @@ def serve_study(args, njobs):
     grid, P = 4, 16
     rng = np.random.default_rng(3)
     arrivals = np.cumsum(rng.exponential(1.0 / args.rate, njobs))
-    sides = rng.choice(SERVE_SIDES if not args.quick else SERVE_SIDES[:7], njobs)
+    side_set = ([int(x) for x in args.serve_sides.split(",")] if args.serve_sides else
+                SERVE_SIDES if not args.quick else SERVE_SIDES[:7])
+    sides = rng.choice(side_set, njobs)
     dtypes = np.where(rng.random(njobs) < 0.5, api.C128, api.C64)
     classes = sorted(set(zip(sides.tolist(), dtypes.tolist())))
     flops = float(sum(2 * flops_per_transform(int(sd) ** 3) for sd in sides))
@@ -784,7 +788,7 @@ def serve_study(args, njobs):
         "served_over_alone": round(served_rate / alone_same["jobs_per_s"], 3),
         "served_over_plain": round(served_rate / alone_plain["jobs_per_s"], 3),
         "roundtrip_rel_l2": errs,
-        "config": {"grid": "4x4 virtual", "sides": SERVE_SIDES if not args.quick else SERVE_SIDES[:7],
+        "config": {"grid": "4x4 virtual", "sides": side_set,
                    "dtypes": "complex64 / complex128, p = 1/2", "seed": 3,
                    "chain": "H2D, block->rotate reshape, split FFT forward, spectrum D2H, inverse, output D2H"},
     }
@@ -1244,6 +1248,8 @@ def main():
     ap.add_argument("--slots", type=int, default=4, help="with --serve: stream slots")
     ap.add_argument("--batch", type=int, default=8, help="with --serve: jobs that may share launches")
     ap.add_argument("--arena-gb", dest="arena_gb", type=int, default=96, help="with --serve: device arena")
+    ap.add_argument("--serve-sides", dest="serve_sides", default="",
+                    help="with --serve: comma-separated cube sides instead of the C5 set")
     ap.add_argument("--mix-side", dest="mix_side", type=int, default=0,
                     help="with --serve: jobs of sides up to this share launches with other sides (0: off)")
     ap.add_argument("--no-extras", dest="no_extras", action="store_true",
