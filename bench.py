@@ -342,6 +342,19 @@ def e2e_pipelined(w, reps, steps):
     return e2e_ms, serial_ms, host_in.numel() * 16, host_out[0].numel() * 16
 
 
+def transform_roof(N, bd64, bddf, peak):
+    """The whole forward transform against the split FFT's algorithmic bytes, 4 N s (two HBM round trips, the
+    reshapes and the twiddle fused), and against the FP64 pipe (5 N log2 N flops)."""
+    out = {"algorithmic_bytes": 4 * N * 16, "flops": flops_per_transform(N)}
+    for key, bd in (("fp64", bd64), ("double_float", bddf)):
+        t = bd["fft_forward"] * 1e-3
+        gbs = 4 * N * 16 / t / 1e9
+        out[key] = {"forward_ms": round(bd["fft_forward"], 3), "achieved_gbs": round(gbs, 1),
+                    "hbm_frac": round(gbs / peak, 4),
+                    "fp64_pipe_frac": round(flops_per_transform(N) / t / 1e12 / FP64_PEAK_TFLOPS, 4)}
+    return out
+
+
 def run_gpu(args):
     import torch
 
@@ -399,6 +412,7 @@ def run_gpu(args):
     l64, avg64, ach64, tf64 = pass_roof(bd64)
     ldf, avgdf, achdf, tfdf = pass_roof(bddf)
     plans = {"reshape": [w.r01.describe(), w.r12.describe()], "split": sp.describe()}
+    w_N = w.N
     wl = w.length
     dat_pitch = w.r12.dest_pitch
     del w, sp
@@ -445,6 +459,7 @@ def run_gpu(args):
         "fft_gflops": round(flops_step / ((bd64["fft_forward"] + bd64["fft_inverse"]) * 1e-3) / 1e9, 2),
         "reshape_gbs": round(reshape_gbs, 1),
         "reshape_frac_of_hbm": round(reshape_gbs / peak, 4),
+        "transform_roofline": transform_roof(w_N, bd64, bddf, peak),
         "ms_breakdown": {k: round(bd64[k], 3) for k in ("reshapes", "fft_forward", "fft_inverse")},
         "fft_pass_ms": [round(x, 3) for x in l64],
         "roundtrip_rel_l2": rt64,
