@@ -959,7 +959,7 @@ GROUP_SHAPES = [(32, 32, 32), (48, 40, 36), (64, 48, 32), (40, 40, 40), (24, 30,
                 (96, 96, 48), (20, 24, 30)]
 
 
-def group_study(steps=20):
+def group_study(steps=20, graphs=True):
     """Grouped form: the 16 uneven small arrays of GROUP_SHAPES (block decomposition on a 4x4 virtual grid,
     uniform[-1,1) values, seed 5), each transformed forward and back per step, (a) one plan at a time with the
     fixed radix schedules, (b) one plan at a time with the runtime radix schedule PLAN8, (c) all 16 in one
@@ -1015,6 +1015,9 @@ def group_study(steps=20):
             e1.record(stream)
             torch.cuda.synchronize()
             eager = e0.elapsed_time(e1) / steps
+            if not graphs:
+                return {"eager_ms": round(eager, 4),
+                        "eager_transforms_per_s": round(2 * len(plans) / (eager * 1e-3), 1)}
             cap = torch.cuda.Stream(dev)
             cap.wait_stream(stream)
             g = torch.cuda.CUDAGraph()
@@ -1048,7 +1051,8 @@ def group_study(steps=20):
         res["grouped_plan8"]["launches"] = (api.split_group_launches(plans, api.FFTW_FORWARD) +
                                             api.split_group_launches(plans, api.FFTW_BACKWARD))
         res["grouped_over_one_by_one_fixed"] = {
-            k: round(res["one_by_one_fixed_radix"][k] / res["grouped_plan8"][k], 3) for k in ("eager_ms", "graph_ms")}
+            k: round(res["one_by_one_fixed_radix"][k] / res["grouped_plan8"][k], 3)
+            for k in (("eager_ms", "graph_ms") if graphs else ("eager_ms",))}
         out[name] = res
         for sp in plans:
             sp.free()
@@ -1059,7 +1063,7 @@ def group_study(steps=20):
 
 
 def run_group(args):
-    print(json.dumps(group_study(max(args.steps, 10))))
+    print(json.dumps(group_study(max(args.steps, 10), graphs=not args.no_graph)))
 
 
 def compare_study(n=256, ranks=64, trials=10, repeat=10):
@@ -1256,6 +1260,8 @@ def main():
     ap.add_argument("--serve", action="store_true", help="served form: Poisson stream of mixed-size jobs")
     ap.add_argument("--precision", action="store_true", help="precision form: 1024^3 complex64 with error")
     ap.add_argument("--group", action="store_true", help="grouped form: 16 uneven small transforms per launch")
+    ap.add_argument("--no-graph", dest="no_graph", action="store_true",
+                    help="with --group: eager runs only (no CUDA graph capture, e.g. under a profiler)")
     ap.add_argument("--compare", action="store_true",
                     help="slab plan vs autotuned plan at --n (256 by default) on --grid^2 virtual ranks")
     ap.add_argument("--jobs", type=int, default=200, help="with --serve: jobs in the stream")
