@@ -14,7 +14,10 @@
 // split twiddle, and in the split FFT's slot order for whole-dimension
 // passes.  A block steps through its tiles by adding the digits of the grid
 // size to the tile index's mixed-radix digits, and the next tile's address
-// parts load asynchronously behind the current tile's first stage.
+// parts load asynchronously behind the current tile's first stage.  The
+// pass body takes its block index and block count as arguments, so that a
+// grouped launch can give each of several passes (of different plans and
+// lengths) a range of its blocks.
 //
 // Stockham stage with radix r, Lp = product of earlier radices, m = n/(Lp r):
 //   a_q = w_{Lp r}^{j q} * x[j r m + q m + k],  y[(j + s Lp) m + k] = sum_q a_q w_r^{q s}
