@@ -87,6 +87,12 @@ struct dmg_fft_pass {
    * of the other dimensions plus that dimension's table at the coordinate
    * both axes make up */
   int32_t semi_in, semi_out, semi_a, semi_b;
+  /* a separable side (sep_*) whose tile axes semi_a and semi_b lie in one
+   * dimension whose table is the sum of a part along each of its two
+   * sub-axes (tab[y + A z] = tab[y] + tab[A z] - tab[0]): the transform
+   * axis's and the vector axis's entries both count the tile's start in that
+   * dimension, which the side's base takes off once */
+  int32_t pair_in, pair_out;
   struct dmg_fft_layout in, out;
   /* device word set to 1 when a tensor-core pass gave up waiting for its
    * products (NULL: not reported) */

@@ -272,6 +272,21 @@ static void order_by_step(const int64_t *step, int32_t *order) {
 
 /* Geometry of a pass along sub-axis t (of the factors A, B) from layout li
  * to lo. */
+/* whether dimension d's table of a separable layout is the sum of a part
+ * along y and a part along z (x = y + A z, x < L), in its rank part and its
+ * offset part each (so for every rank pitch: the scratch copies of the
+ * layouts differ in pitch only) */
+static int pair_separable(const fft_layout *l, int d, int A, int L) {
+  if (l->ranked || A < 1 || L % A) return 0;
+  const int64_t *t = l->tab[d];
+  const int32_t *r = l->rk[d];
+  for (int x = 0; x < L; ++x) {
+    const int y = x % A, az = x - x % A;
+    if (t[x] - t[y] - t[az] + t[0] != 0 || (int64_t)r[x] - r[y] - r[az] + r[0] != 0) return 0;
+  }
+  return 1;
+}
+
 static int pass_geometry(const struct dmg_split_impl *im, struct dmg_fft_pass *p, int t, const fft_layout *li,
                          const fft_layout *lo, const int *A, const int *B) {
   memset(p, 0, sizeof(*p));
@@ -383,6 +398,20 @@ static int pass_geometry(const struct dmg_split_impl *im, struct dmg_fft_pass *p
       }
   p->semi_in = !distinct && p->semi_a >= 0 && !li->ranked;
   p->semi_out = !distinct && p->semi_a >= 0 && !lo->ranked;
+  /* the shared dimension's table is the sum of a part along each of its
+   * sub-axes (interleaved layouts, blocks holding whole multiples of A): the
+   * side walks as a separable one */
+  if (p->semi_a >= 0) {
+    const int d = p->kdim[p->semi_a];
+    if (p->semi_in && pair_separable(li, d, A[d], im->L[d])) {
+      p->semi_in = 0;
+      p->sep_in = p->pair_in = 1;
+    }
+    if (p->semi_out && pair_separable(lo, d, A[d], im->L[d])) {
+      p->semi_out = 0;
+      p->sep_out = p->pair_out = 1;
+    }
+  }
   return DMG_OK;
 }
 
@@ -436,6 +465,8 @@ static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 static int t0_rel32(const fft_layout *l, const struct dmg_fft_pass *p) {
   if (l->ranked) return 0;
   const int d0 = p->kdim[0];
+  /* (a vector axis in the same dimension moves the table's start per tile) */
+  if (p->kdim[1] == d0 || p->kdim[2] == d0) return 0;
   for (int b = 0; b < p->nbatch; ++b)
     if ((p->bsub[b] >> 1) == d0) return 0;
   const int mult0 = p->kisz[0] ? p->A[d0] : 1;
@@ -613,7 +644,9 @@ static int impl_upload(struct dmg_split_impl *im) {
 /* Forward and inverse pass lists of the split schedule. */
 /* how a pass side is addressed: separable over the tile axes, two axes in
  * one dimension, or per value */
-static const char *side_kind(int sep, int semi) { return sep ? "" : (semi ? "(shared dim)" : "(per value)"); }
+static const char *side_kind(int sep, int semi, int pair) {
+  return pair ? "(paired)" : sep ? "" : (semi ? "(shared dim)" : "(per value)");
+}
 
 /* A pass's tile axes fastest first in memory, as letters: t the transform
  * axis, a and b the first and second vector axes. */
@@ -693,8 +726,8 @@ static int build_passes_split(struct dmg_split_impl *im) {
     axis_letters(p->store_order, so);
     pos += snprintf(im->desc + pos, sizeof(im->desc) - pos,
                     " [t=%d n=%d v1=%d x%d v2=%d x%d tiles=%lld%s in=%s%s out=%s%s]", p->t, p->n, p->v1, p->M1, p->v2,
-                    p->M2, (long long)p->ntiles, p->twiddle ? " tw" : "", lo, side_kind(p->sep_in, p->semi_in), so,
-                    side_kind(p->sep_out, p->semi_out));
+                    p->M2, (long long)p->ntiles, p->twiddle ? " tw" : "", lo, side_kind(p->sep_in, p->semi_in, p->pair_in), so,
+                    side_kind(p->sep_out, p->semi_out, p->pair_out));
   }
   return DMG_OK;
 }
@@ -773,8 +806,8 @@ static int build_passes_line(struct dmg_split_impl *im) {
     pos += snprintf(im->desc + pos, sizeof(im->desc) - pos,
                     " [d=%d n=%d v1=%d x%d v2=%d x%d tiles=%lld%s in=%s%s out=%s%s]", p->t / 2, p->n,
                     p->v1 >= 0 ? p->v1 / 2 : -1, p->M1, p->v2 >= 0 ? p->v2 / 2 : -1, p->M2, (long long)p->ntiles,
-                    p->perm_out ? " slots" : "", lo, side_kind(p->sep_in, p->semi_in), so,
-                    side_kind(p->sep_out, p->semi_out));
+                    p->perm_out ? " slots" : "", lo, side_kind(p->sep_in, p->semi_in, p->pair_in), so,
+                    side_kind(p->sep_out, p->semi_out, p->pair_out));
   }
   return DMG_OK;
 }

@@ -1009,16 +1009,23 @@ __device__ __forceinline__ void copy_async_wait_all() { asm volatile("cp.async.w
 // entries, asynchronously; part has parts_len entries): part[1 + c] and
 // part[1 + M1 + c] the entries of the v1 and v2 dimensions (0 past the tile's
 // extent), part[1 + M1 + M2 + u] that of dimension u when no tile axis
-// covers it (else 0).  The side's address is then L.base + the last three +
-// the tables of the tile axes.
+// covers it (else 0), and part[0] the paired dimension's entry at the
+// tile's start (pair: that dimension holds two tile axes and a sum of parts
+// along them; else 0).  The side's address is then L.base + the last three
+// - part[0] + the tables of the tile axes.
 __device__ __forceinline__ void sep_parts_async(const dmg_fft_layout &L, const dmg_fft_pass &p, const int *yb,
                                                 const int *zb, int lim1, int lim2, int tid, int64_t *part,
-                                                bool semi = false) {
+                                                bool semi = false, bool pair = false) {
   const int M1 = p.M1;
   const int E = 1 + M1 + p.M2;
   for (int i = tid; i < E + 3; i += NT) {
     if (i == 0) {
-      part[0] = 0;
+      if (pair) {
+        const int d = p.kdim[p.semi_a];
+        copy_async<8>(part, L.tab[d] + (yb[d] + p.A[d] * zb[d]));
+      } else {
+        part[0] = 0;
+      }
     } else if (i >= E) {
       const int d = i - E;
       if (d < p.ndim && d != p.kdim[0] && d != p.kdim[1] && d != p.kdim[2])
@@ -1069,7 +1076,7 @@ __device__ __forceinline__ int64_t shared_dim_part(const SharedDim &s, const dmg
 // the base of a separable side's addresses in a tile (parts complete)
 __device__ __forceinline__ int64_t sep_base(const dmg_fft_layout &L, const dmg_fft_pass &p, const int64_t *part) {
   const int E = 1 + p.M1 + p.M2;
-  return L.base + part[E] + part[E + 1] + part[E + 2];
+  return L.base + part[E] + part[E + 1] + part[E + 2] - part[0];
 }
 
 // ---------------------------------------------------------------- the pass kernel
@@ -1738,9 +1745,10 @@ __device__ __forceinline__ void pass_body(const dmg_fft_pass &p, const dmg_fft_b
     }
     if (bid < ntiles_all) {
       const TileState &st = kc.ts[0];
-      if (p.sep_in || p.semi_in) sep_parts_async(p.in, p, st.yb, st.zb, st.lim1, st.lim2, tid, parts_in, p.semi_in);
+      if (p.sep_in || p.semi_in)
+        sep_parts_async(p.in, p, st.yb, st.zb, st.lim1, st.lim2, tid, parts_in, p.semi_in, p.pair_in);
       if (p.sep_out || p.semi_out)
-        sep_parts_async(p.out, p, st.yb, st.zb, st.lim1, st.lim2, tid, parts_out0, p.semi_out);
+        sep_parts_async(p.out, p, st.yb, st.zb, st.lim1, st.lim2, tid, parts_out0, p.semi_out, p.pair_out);
       copy_async_commit();
     }
   }
@@ -1765,10 +1773,10 @@ __device__ __forceinline__ void pass_body(const dmg_fft_pass &p, const dmg_fft_b
     if (next < ntiles_all) {
       const TileState &sn = kc.ts[nxt];
       if (p.sep_in || p.semi_in)
-        sep_parts_async(p.in, p, sn.yb, sn.zb, sn.lim1, sn.lim2, tid, parts_in, p.semi_in);
+        sep_parts_async(p.in, p, sn.yb, sn.zb, sn.lim1, sn.lim2, tid, parts_in, p.semi_in, p.pair_in);
       if (p.sep_out || p.semi_out)
         sep_parts_async(p.out, p, sn.yb, sn.zb, sn.lim1, sn.lim2, tid, parts_out0 + ((it + 1) & 1) * parts_len(p),
-                        p.semi_out);
+                        p.semi_out, p.pair_out);
       copy_async_commit();
     }
     // convert a complex128 input to double-float, apply the inverse split
