@@ -63,7 +63,10 @@ struct dmg_fft_pass {
    * 0 none; 1 multiply after the transform by exp(-2 pi i y_d k_d / L_d);
    * 2 multiply by its conjugate before the transform */
   int32_t twiddle;
-  const void *tw[DMG_FFT_MAXDIM]; /* per dim: L_d roots exp(-2 pi i m / L_d) */
+  /* per dim: the split twiddles exp(-2 pi i y k / L_d) (y < A_d, k < B_d)
+   * at k * A_d + y (twk) and at y * B_d + k (twy), so that lanes stepping
+   * along either read neighbouring entries */
+  const void *twk[DMG_FFT_MAXDIM], *twy[DMG_FFT_MAXDIM];
   /* double-float passes (dtype 2): whether the input / output is stored as
    * complex128 (converted at load / store, scaled by 2^-E / 2^E) rather
    * than as double-float pairs; E = *scale_exp */

@@ -511,7 +511,7 @@ static int impl_upload(struct dmg_split_impl *im) {
     if (all[k]->ranked) bytes += align256((size_t)nd * all[k]->nranks * 8);
   }
   for (int k = 0; k < im->nfwd; ++k) bytes += align256((size_t)im->fwd[k].p.n * cs);
-  for (int d = 0; d < nd; ++d) bytes += align256((size_t)im->L[d] * cs);
+  for (int d = 0; d < nd; ++d) bytes += 2 * align256((size_t)im->L[d] * cs);
   bytes += 256; /* scale exponent */
   char *host = (char *)calloc(1, bytes + 256);
   if (!host) return dmg_error(DMG_ERR_NOMEM, "split plan: out of host memory for the device tables");
@@ -566,27 +566,36 @@ static int impl_upload(struct dmg_split_impl *im) {
     roots_dev[k] = (char *)dev + pos;
     pos += align256((size_t)n * cs);
   }
-  const void *tw_dev[DMG_FFT_MAXDIM] = {NULL, NULL, NULL};
+  /* split twiddles exp(-2 pi i y k / L) for y < A, k < B, in two orders:
+   * k-major (entry k A + y) and y-major (entry y B + k) */
+  const void *twk_dev[DMG_FFT_MAXDIM] = {NULL, NULL, NULL}, *twy_dev[DMG_FFT_MAXDIM] = {NULL, NULL, NULL};
   for (int d = 0; d < nd; ++d) {
-    for (int m = 0; m < im->L[d]; ++m) {
-      double re, iv;
-      twiddle_value(m, im->L[d], &re, &iv);
-      if (im->arith == DMG_ARITH_DF) {
-        float *f = (float *)(host + pos) + 4 * m;
-        f[0] = (float)re;
-        f[1] = (float)iv;
-        f[2] = (float)(re - (double)f[0]);
-        f[3] = (float)(iv - (double)f[1]);
-      } else if (cs == 16) {
-        ((double *)(host + pos))[2 * m] = re;
-        ((double *)(host + pos))[2 * m + 1] = iv;
-      } else {
-        ((float *)(host + pos))[2 * m] = (float)re;
-        ((float *)(host + pos))[2 * m + 1] = (float)iv;
+    const int A = im->A[d], B = im->B[d];
+    for (int order = 0; order < 2; ++order) {
+      for (int y = 0; y < A; ++y) {
+        for (int k = 0; k < B; ++k) {
+          const int e = order == 0 ? k * A + y : y * B + k;
+          double re, iv;
+          twiddle_value((long long)y * k, im->L[d], &re, &iv);
+          if (im->arith == DMG_ARITH_DF) {
+            float *f = (float *)(host + pos) + 4 * e;
+            f[0] = (float)re;
+            f[1] = (float)iv;
+            f[2] = (float)(re - (double)f[0]);
+            f[3] = (float)(iv - (double)f[1]);
+          } else if (cs == 16) {
+            ((double *)(host + pos))[2 * e] = re;
+            ((double *)(host + pos))[2 * e + 1] = iv;
+          } else {
+            ((float *)(host + pos))[2 * e] = (float)re;
+            ((float *)(host + pos))[2 * e + 1] = (float)iv;
+          }
+        }
       }
+      if (order == 0) twk_dev[d] = (char *)dev + pos;
+      else twy_dev[d] = (char *)dev + pos;
+      pos += align256((size_t)im->L[d] * cs);
     }
-    tw_dev[d] = (char *)dev + pos;
-    pos += align256((size_t)im->L[d] * cs);
   }
   im->d_scale = (int32_t *)((char *)dev + pos);
   im->d_status = im->d_scale + 1; /* zero from the upload */
@@ -606,7 +615,10 @@ static int impl_upload(struct dmg_split_impl *im) {
     for (int k = 0; k < cnt; ++k) {
       int fk = dir == 0 ? k : im->nfwd - 1 - k; /* the inverse mirrors the forward list */
       list[k].p.roots = roots_dev[fk];
-      for (int d = 0; d < DMG_FFT_MAXDIM; ++d) list[k].p.tw[d] = tw_dev[d];
+      for (int d = 0; d < DMG_FFT_MAXDIM; ++d) {
+        list[k].p.twk[d] = twk_dev[d];
+        list[k].p.twy[d] = twy_dev[d];
+      }
       /* double-float runs keep float pairs between passes: only the first
        * pass reads complex128 and only the last writes it */
       list[k].p.in_fp64 = im->arith == DMG_ARITH_DF && k == 0;

@@ -1107,6 +1107,7 @@ constexpr int NDIG = 9;
 // the FFT stages.
 struct PassConsts {
   int ld, M1, d0, mult0, td, v1_ytd, v2_ytd, in64, out64;
+  int tw_kmaj;  // the store walk steps along y first: read the k-major twiddle table
   unsigned buf_a, buf_b, roots_off, contrib_off, spos_off, t0_off;
   int t0_in, t0_out;              // the sides whose transform-axis offsets are in shared memory
   int64_t t0base_in, t0base_out;  // their first entries
@@ -1674,6 +1675,7 @@ __device__ __forceinline__ void pass_body(const dmg_fft_pass &p, const dmg_fft_b
     kc.td = td;
     kc.v1_ytd = p.kdim[1] == td && !p.kisz[1];
     kc.v2_ytd = p.kdim[2] == td && !p.kisz[2];
+    kc.tw_kmaj = (p.store_order[0] == 1 && kc.v1_ytd) || (p.store_order[0] == 2 && kc.v2_ytd);
     kc.in64 = p.in_fp64 != 0;
     kc.out64 = p.out_fp64 != 0;
     // this block's first two tiles, and the digits of the stride between its tiles
@@ -1789,7 +1791,7 @@ __device__ __forceinline__ void pass_body(const dmg_fft_pass &p, const dmg_fft_b
       const TileState &st = kc.ts[cur];
       const int lim1 = st.lim1, lim2 = st.lim2;
       const int sexp = st.sexp;
-      const C2<T> *twt = reinterpret_cast<const C2<T> *>(p.tw[kc.td]);
+      const C2<T> *twt = reinterpret_cast<const C2<T> *>(p.twy[kc.td]);  // lanes step along k
       C2<T> *stg = reinterpret_cast<C2<T> *>(sm);
       const int total = n * M1 * p.M2;
       for (int e = tid; e < total; e += NT) {
@@ -1810,8 +1812,8 @@ __device__ __forceinline__ void pass_body(const dmg_fft_pass &p, const dmg_fft_b
           v = stg[sp];
         }
         if (p.twiddle == 2) {
-          const int ex = (st.ytw + (kc.v1_ytd ? c1 : 0) + (kc.v2_ytd ? c2 : 0)) * i;
-          if (ex) v = mul<T>(v, conj<T>(twt[ex]));
+          const int y = st.ytw + (kc.v1_ytd ? c1 : 0) + (kc.v2_ytd ? c2 : 0);
+          if (y && i) v = mul<T>(v, conj<T>(twt[y * n + i]));
         }
         stg[sp] = v;
       }
@@ -1904,7 +1906,10 @@ __device__ __forceinline__ void pass_body(const dmg_fft_pass &p, const dmg_fft_b
       const bool out64 = kc.out64;
       const int sexp = st.sexp;
       void *dst = bt.dst[st.job];
-      const C2<T> *twt = reinterpret_cast<const C2<T> *>(p.tw[kc.td]);
+      // split twiddle of output (y, k = c0): entry k A + y or y n + k, whichever the walk's lanes step along
+      const bool kmaj = kc.tw_kmaj;
+      const C2<T> *twt = reinterpret_cast<const C2<T> *>(kmaj ? p.twk[kc.td] : p.twy[kc.td]);
+      const int twA = kmaj ? p.A[kc.td] : 1, twB = kmaj ? 1 : n;
       const bool tw1 = p.twiddle == 1;
       const int ytw = st.ytw, v1y = kc.v1_ytd, v2y = kc.v2_ytd;
       bool done = p.sep_out &&
@@ -1912,8 +1917,8 @@ __device__ __forceinline__ void pass_body(const dmg_fft_pass &p, const dmg_fft_b
                                       [&](int64_t ad, int sp, int c0, int c1, int c2) {
                                     C2<T> x = res[sp];
                                     if (tw1) {
-                                      const int ex = (ytw + (v1y ? c1 : 0) + (v2y ? c2 : 0)) * c0;
-                                      if (ex) x = mul<T>(x, twt[ex]);
+                                      const int y = ytw + (v1y ? c1 : 0) + (v2y ? c2 : 0);
+                                      if (y && c0) x = mul<T>(x, twt[c0 * twA + y * twB]);
                                     }
                                     store_elem<T>(dst, ad, x, out64, sexp);
                                   },
@@ -1932,9 +1937,9 @@ __device__ __forceinline__ void pass_body(const dmg_fft_pass &p, const dmg_fft_b
           if (ok[u]) {
             const int c0 = w.coord(p.store_pos[0]), c1 = w.coord(p.store_pos[1]), c2 = w.coord(p.store_pos[2]);
             C2<T> x = res[(c1 + M1 * c2) * ld + spos[c0]];
-            if (p.twiddle == 1) {
-              const int ex = (st.ytw + (kc.v1_ytd ? c1 : 0) + (kc.v2_ytd ? c2 : 0)) * c0;
-              if (ex) x = mul<T>(x, twt[ex]);
+            if (tw1) {
+              const int y = ytw + (v1y ? c1 : 0) + (v2y ? c2 : 0);
+              if (y && c0) x = mul<T>(x, twt[c0 * twA + y * twB]);
             }
             v[u] = x;
             if (p.sep_out) {
