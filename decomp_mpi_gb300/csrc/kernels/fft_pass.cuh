@@ -1907,9 +1907,9 @@ __device__ __forceinline__ void pass_body(const dmg_fft_pass &p, const dmg_fft_b
       const int sexp = st.sexp;
       void *dst = bt.dst[st.job];
       // split twiddle of output (y, k = c0): entry k A + y or y n + k, whichever the walk's lanes step along
-      const bool kmaj = kc.tw_kmaj;
-      const C2<T> *twt = reinterpret_cast<const C2<T> *>(kmaj ? p.twk[kc.td] : p.twy[kc.td]);
-      const int twA = kmaj ? p.A[kc.td] : 1, twB = kmaj ? 1 : n;
+      // (the table's order and A are re-read where a twiddle is due, so that no register holds them
+      // through the walks)
+      const C2<T> *twt = reinterpret_cast<const C2<T> *>(kc.tw_kmaj ? p.twk[kc.td] : p.twy[kc.td]);
       const bool tw1 = p.twiddle == 1;
       const int ytw = st.ytw, v1y = kc.v1_ytd, v2y = kc.v2_ytd;
       bool done = p.sep_out &&
@@ -1918,7 +1918,8 @@ __device__ __forceinline__ void pass_body(const dmg_fft_pass &p, const dmg_fft_b
                                     C2<T> x = res[sp];
                                     if (tw1) {
                                       const int y = ytw + (v1y ? c1 : 0) + (v2y ? c2 : 0);
-                                      if (y && c0) x = mul<T>(x, twt[c0 * twA + y * twB]);
+                                      if (y && c0)
+                                        x = mul<T>(x, twt[kc.tw_kmaj ? c0 * p.A[kc.td] + y : y * n + c0]);
                                     }
                                     store_elem<T>(dst, ad, x, out64, sexp);
                                   },
@@ -1939,7 +1940,7 @@ __device__ __forceinline__ void pass_body(const dmg_fft_pass &p, const dmg_fft_b
             C2<T> x = res[(c1 + M1 * c2) * ld + spos[c0]];
             if (tw1) {
               const int y = ytw + (v1y ? c1 : 0) + (v2y ? c2 : 0);
-              if (y && c0) x = mul<T>(x, twt[c0 * twA + y * twB]);
+              if (y && c0) x = mul<T>(x, twt[kc.tw_kmaj ? c0 * p.A[kc.td] + y : y * n + c0]);
             }
             v[u] = x;
             if (p.sep_out) {
