@@ -113,7 +113,8 @@ static int time_candidate(tune_ctx *c, SplitPlan cand) {
 static void refine(tune_ctx *c) {
   SplitPlan b = c->best;
   if (!b) return;
-  const int base = DMG_FFT_TILE_TARGET(c->dtype == DMG_C128 ? 16 : 8);
+  const int base = dmg_split_get_arith(b) == DMG_ARITH_FP64 ? DMG_FFT_TILE_TARGET_FP64
+                                                            : DMG_FFT_TILE_TARGET(c->dtype == DMG_C128 ? 16 : 8);
   const int tiles[2] = {base / 2, 2 * base};
   for (int i = 0; i < 2; ++i) {
     const int keep = dmg_split_get_tile(b);

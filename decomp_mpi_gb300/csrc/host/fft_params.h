@@ -115,6 +115,16 @@ struct dmg_fft_pass {
 #ifndef DMG_FFT_TILE_TARGET
 #define DMG_FFT_TILE_TARGET(es) ((es) == 8 ? 4096 : 2048)
 #endif
+/* Native FP64 passes (complex128): 128-thread blocks, three per SM, with
+ * tiles of 1024 values.  The passes are bound by the FP64 pipe; more and
+ * smaller blocks keep it busier while other blocks gather, scatter or wait
+ * at a barrier (about 4 % faster than two 256-thread blocks with 2048-value
+ * tiles at 512^3).  The FP64 translation units compile the pass kernel with
+ * these sizes and the planner gives FP64 passes tiles of at most this many
+ * values (a whole line where a line is longer). */
+#define DMG_FFT_FP64_NT 128
+#define DMG_FFT_FP64_MINB 3
+#define DMG_FFT_TILE_TARGET_FP64 1024
 /* Wide passes: one 512-thread block per SM with tiles of twice the values,
  * so that passes whose lines are strided in memory move rows twice as long
  * (FP32 and double-float power-of-two lengths; the plan's tile size asks for

@@ -328,6 +328,10 @@ static int pass_geometry(const struct dmg_split_impl *im, struct dmg_fft_pass *p
    * length from 256 to 2048, compile-time radix schedule, not the
    * tensor-core 1024-point stage, whose products take four lines) */
   int target = im->tile_values > 0 ? im->tile_values : DMG_FFT_TILE_TARGET(im->esize);
+  /* native FP64 passes run in smaller blocks with tiles of at most
+   * DMG_FFT_TILE_TARGET_FP64 values */
+  if (im->arith == DMG_ARITH_FP64 && (im->tile_values == 0 || target > DMG_FFT_TILE_TARGET_FP64))
+    target = DMG_FFT_TILE_TARGET_FP64;
   /* (the wide kernels' shared memory holds their tiles for lines of 256
    * points or more; shorter lines pad and tabulate too much per tile) */
   const int pow2n = p->n >= 256 && p->n <= 2048 && (p->n & (p->n - 1)) == 0;

@@ -677,9 +677,15 @@ __host__ __device__ constexpr int fixed_radix(int nf, int lp) {
 __host__ __device__ constexpr bool pow2_length(int n) { return n >= 8 && n <= 2048 && (n & (n - 1)) == 0; }
 __host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n >> 1); }
 // bytes per stage buffer of a power-of-two length kernel: the largest tile
-// of the pass in the line-padded layout
+// of the pass in the line-padded layout (one line where a line is longer
+// than the tile target)
 __host__ __device__ constexpr size_t pow2_stride(size_t es, int n) {
-  return ((size_t)(DMG_FFT_TILE_TARGET(es) / n) * (size_t)(n | 1) * es + 15) & ~(size_t)15;
+  return ((size_t)(DMG_FFT_TILE_TARGET(es) / n > 0 ? DMG_FFT_TILE_TARGET(es) / n : 1) * (size_t)(n | 1) * es + 15) &
+         ~(size_t)15;
+}
+// the most lines side by side a power-of-two length kernel's buffers hold
+__host__ __device__ constexpr int pow2_lines(size_t es, int n) {
+  return DMG_FFT_TILE_TARGET(es) / n > 0 ? DMG_FFT_TILE_TARGET(es) / n : 1;
 }
 template <typename T, int NF, int LPC>  // LPC: the consuming stage's LP
 struct HopSwz {
