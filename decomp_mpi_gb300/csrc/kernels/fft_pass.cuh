@@ -738,13 +738,61 @@ __device__ __forceinline__ void pow2_twiddles(const C2<T> *roots, C2<T> *tws, in
   }
 }
 
+// FP64 radix-8 stage with its input twiddles w^q (w = w_{8 LP}^j), as three
+// layers of radix-2 butterflies y0 = a + t b, y1 = 2 a - y0 whose twiddle t
+// is a single complex number: six FMAs per butterfly, 72 per eight values
+// against 80 for seven twiddle products and the 8-point DFT.  With
+// A_q = x_q + w^4 x_{q+4} (B: minus), the even outputs are the 4-point DFT of
+// w^q A_q and the odd ones that of (w W8)^q B_q; the same split again leaves
+// twiddles w^2 and w^2 W4 for the second layer and w, w W4, w W8, w W8 W4 for
+// the third (W8 = w_8 in the transform's direction, W4 = W8^2: multiplying by
+// it is a swap and a sign).  v = w W8 comes from the pass's root table.
+template <int SIGN>
+__device__ __forceinline__ void bfly_tw(double2 &a, double2 &b, double tx, double ty) {
+  const double y0x = __fma_rn(tx, b.x, __fma_rn(-ty, b.y, a.x));
+  const double y0y = __fma_rn(tx, b.y, __fma_rn(ty, b.x, a.y));
+  b.x = __fma_rn(2.0, a.x, -y0x);
+  b.y = __fma_rn(2.0, a.y, -y0y);
+  a.x = y0x;
+  a.y = y0y;
+}
+// the same with twiddle t W4
+template <int SIGN>
+__device__ __forceinline__ void bfly_tw_rot(double2 &a, double2 &b, double tx, double ty) {
+  if (SIGN < 0) {
+    bfly_tw<SIGN>(a, b, ty, -tx);  // t (-i)
+  } else {
+    bfly_tw<SIGN>(a, b, -ty, tx);  // t i
+  }
+}
+template <int SIGN>
+__device__ __forceinline__ void dft8_tw_fma(double2 *a, double2 w1, double2 w2, double2 w4, double2 v) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q) bfly_tw<SIGN>(a[q], a[q + 4], w4.x, w4.y);
+  bfly_tw<SIGN>(a[0], a[2], w2.x, w2.y);
+  bfly_tw<SIGN>(a[1], a[3], w2.x, w2.y);
+  bfly_tw_rot<SIGN>(a[4], a[6], w2.x, w2.y);
+  bfly_tw_rot<SIGN>(a[5], a[7], w2.x, w2.y);
+  bfly_tw<SIGN>(a[0], a[1], w1.x, w1.y);
+  bfly_tw_rot<SIGN>(a[2], a[3], w1.x, w1.y);
+  bfly_tw<SIGN>(a[4], a[5], v.x, v.y);
+  bfly_tw_rot<SIGN>(a[6], a[7], v.x, v.y);
+  // outputs in bit-reversed places: y0 y4 y2 y6 y1 y5 y3 y7
+  const double2 y1 = a[4], y2 = a[2], y3 = a[6], y4 = a[1], y6 = a[3];
+  a[1] = y1;
+  a[2] = y2;
+  a[3] = y3;
+  a[4] = y4;
+  a[6] = y6;
+}
+
 // The Stockham stage after the first LP points of a power-of-two NF: from
 // the line-padded staging layout (first stage) or the previous stage's
 // swizzled layout, to the next stage's swizzled layout or (last stage) the
 // line-padded layout the scatter reads.  tws: the tables above.
 template <typename T, int SIGN, int NF, int LP>
 __device__ __forceinline__ void stage_pow2(const C2<T> *in, C2<T> *out, const C2<T> *tws, int nlines, int ld, int tid,
-                                           bool conv, int sexp) {
+                                           bool conv, int sexp, const C2<T> *groots = nullptr) {
   constexpr int R = fixed_radix(NF, LP);
   constexpr int NR = NF / R;
   constexpr int M = NR / LP;
@@ -761,7 +809,26 @@ __device__ __forceinline__ void stage_pow2(const C2<T> *in, C2<T> *out, const C2
     const int j = bb >> LGM;
     const int k = bb & (M - 1);
     C2<T> a[R];
-    if constexpr (IN_SWZ) {
+    constexpr bool FMA8 = std::is_same<T, double>::value && R == 8 && IN_SWZ;
+    if constexpr (FMA8) {
+      // native FP64, twiddled radix 8: the twiddles go into the butterflies
+      const int gxb = Gin::g((l << LGNF) + j * R * M + k) * ES;
+#pragma unroll
+      for (int q = 0; q < R; ++q) a[q] = at_xor<T>(in, gxb, Gin::g(q * M) * ES);
+      constexpr int TSTEP = NF / (LP * R);
+      C2<T> w1, w2, w4;
+      if constexpr (global_twiddles(NF, sizeof(C2<T>))) {
+        w1 = root_at<T, SIGN>(tws, j * TSTEP);
+        w2 = root_at<T, SIGN>(tws, 2 * j * TSTEP);
+        w4 = root_at<T, SIGN>(tws, 4 * j * TSTEP);
+      } else {
+        w1 = tw[j];
+        w2 = tw[LP + j];
+        w4 = tw[3 * LP + j];
+      }
+      const C2<T> v = root_at<T, SIGN>(groots, j * TSTEP + NF / 8);
+      dft8_tw_fma<SIGN>(a, w1, w2, w4, v);
+    } else if constexpr (IN_SWZ) {
       const int gxb = Gin::g((l << LGNF) + j * R * M + k) * ES;
 #pragma unroll
       for (int q = 0; q < R; ++q) {
@@ -796,7 +863,7 @@ __device__ __forceinline__ void stage_pow2(const C2<T> *in, C2<T> *out, const C2
         a[q] = v;
       }
     }
-    bfly_fixed<T, SIGN, R>(a);
+    if constexpr (!FMA8) bfly_fixed<T, SIGN, R>(a);
     if constexpr (OUT_SWZ) {
       const int gyb = Gout::g((l << LGNF) + bb) * ES;
 #pragma unroll
@@ -861,14 +928,14 @@ __device__ __forceinline__ void stage_fixed(const C2<T> *in, C2<T> *out, const C
 // `spare`; returns the buffer holding the result.
 template <typename T, int SIGN, int NF, int LP>
 __device__ __forceinline__ C2<T> *stages_fixed(C2<T> *in, C2<T> *out, C2<T> *spare, const C2<T> *roots, int nlines,
-                                               int ld, int tid) {
+                                               int ld, int tid, const C2<T> *groots = nullptr) {
   if constexpr (LP < NF) {
     if constexpr (pow2_length(NF)) {
-      stage_pow2<T, SIGN, NF, LP>(in, out, roots, nlines, ld, tid, false, 0);
+      stage_pow2<T, SIGN, NF, LP>(in, out, roots, nlines, ld, tid, false, 0, groots);
     } else {
       stage_fixed<T, SIGN, NF, LP>(in, out, roots, nlines, ld, tid);
     }
-    return stages_fixed<T, SIGN, NF, LP * fixed_radix(NF, LP)>(out, spare, out, roots, nlines, ld, tid);
+    return stages_fixed<T, SIGN, NF, LP * fixed_radix(NF, LP)>(out, spare, out, roots, nlines, ld, tid, groots);
   } else {
     (void)out;
     (void)spare;
@@ -1874,8 +1941,8 @@ __device__ __forceinline__ void pass_body(const dmg_fft_pass &p, const dmg_fft_b
                                                                       : reinterpret_cast<const C2<T> *>(sm + 3 * PSTRIDE))
                            : DMG_FFT_SMEM_ROOTS ? reinterpret_cast<const C2<T> *>(sm + kc.roots_off)
                                                 : reinterpret_cast<const C2<T> *>(p.roots);
-        res = stages_fixed<T, SIGN, NF, fixed_radix(NF, 1)>(bufA, bufB, bufA, rts,
-                                                            nlines, ld, tid);
+        res = stages_fixed<T, SIGN, NF, fixed_radix(NF, 1)>(bufA, bufB, bufA, rts, nlines, ld, tid,
+                                                            reinterpret_cast<const C2<T> *>(p.roots));
       } else {
         const C2<T> *groots = reinterpret_cast<const C2<T> *>(p.roots);
         C2<T> *in = bufA, *out = bufB;
