@@ -786,6 +786,19 @@ __device__ __forceinline__ void dft8_tw_fma(double2 *a, double2 w1, double2 w2, 
   a[6] = y6;
 }
 
+// The radix-4 stage the same way: A_q = x_q + w^2 x_{q+2} (B: minus), then
+// y0, y2 = A_0 +- w A_1 and y1, y3 = B_0 +- w W4 B_1 (24 FMAs against 28).
+template <int SIGN>
+__device__ __forceinline__ void dft4_tw_fma(double2 *a, double2 w1, double2 w2) {
+  bfly_tw<SIGN>(a[0], a[2], w2.x, w2.y);
+  bfly_tw<SIGN>(a[1], a[3], w2.x, w2.y);
+  bfly_tw<SIGN>(a[0], a[1], w1.x, w1.y);
+  bfly_tw_rot<SIGN>(a[2], a[3], w1.x, w1.y);
+  const double2 y1 = a[2];  // y0 y2 y1 y3 in place
+  a[2] = a[1];
+  a[1] = y1;
+}
+
 // The Stockham stage after the first LP points of a power-of-two NF: from
 // the line-padded staging layout (first stage) or the previous stage's
 // swizzled layout, to the next stage's swizzled layout or (last stage) the
@@ -809,25 +822,28 @@ __device__ __forceinline__ void stage_pow2(const C2<T> *in, C2<T> *out, const C2
     const int j = bb >> LGM;
     const int k = bb & (M - 1);
     C2<T> a[R];
-    constexpr bool FMA8 = std::is_same<T, double>::value && R == 8 && IN_SWZ;
+    constexpr bool FMA8 = std::is_same<T, double>::value && (R == 8 || R == 4) && IN_SWZ;
     if constexpr (FMA8) {
-      // native FP64, twiddled radix 8: the twiddles go into the butterflies
+      // native FP64, twiddled radix 8 or 4: the twiddles go into the butterflies
       const int gxb = Gin::g((l << LGNF) + j * R * M + k) * ES;
 #pragma unroll
       for (int q = 0; q < R; ++q) a[q] = at_xor<T>(in, gxb, Gin::g(q * M) * ES);
       constexpr int TSTEP = NF / (LP * R);
-      C2<T> w1, w2, w4;
+      C2<T> w1, w2;
       if constexpr (global_twiddles(NF, sizeof(C2<T>))) {
         w1 = root_at<T, SIGN>(tws, j * TSTEP);
         w2 = root_at<T, SIGN>(tws, 2 * j * TSTEP);
-        w4 = root_at<T, SIGN>(tws, 4 * j * TSTEP);
       } else {
         w1 = tw[j];
         w2 = tw[LP + j];
-        w4 = tw[3 * LP + j];
       }
-      const C2<T> v = root_at<T, SIGN>(groots, j * TSTEP + NF / 8);
-      dft8_tw_fma<SIGN>(a, w1, w2, w4, v);
+      if constexpr (R == 8) {
+        const C2<T> w4 = global_twiddles(NF, sizeof(C2<T>)) ? root_at<T, SIGN>(tws, 4 * j * TSTEP) : tw[3 * LP + j];
+        const C2<T> v = root_at<T, SIGN>(groots, j * TSTEP + NF / 8);
+        dft8_tw_fma<SIGN>(a, w1, w2, w4, v);
+      } else {
+        dft4_tw_fma<SIGN>(a, w1, w2);
+      }
     } else if constexpr (IN_SWZ) {
       const int gxb = Gin::g((l << LGNF) + j * R * M + k) * ES;
 #pragma unroll
