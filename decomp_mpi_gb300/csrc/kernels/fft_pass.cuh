@@ -509,6 +509,67 @@ __device__ __forceinline__ C2<T> root_at(const C2<T> *roots, int i) {
   return SIGN > 0 ? conj<T>(w) : w;
 }
 
+// FP64 radix-8 stage with its input twiddles w^q (w = w_{8 LP}^j), as three
+// layers of radix-2 butterflies y0 = a + t b, y1 = 2 a - y0 whose twiddle t
+// is a single complex number: six FMAs per butterfly, 72 per eight values
+// against 80 for seven twiddle products and the 8-point DFT.  With
+// A_q = x_q + w^4 x_{q+4} (B: minus), the even outputs are the 4-point DFT of
+// w^q A_q and the odd ones that of (w W8)^q B_q; the same split again leaves
+// twiddles w^2 and w^2 W4 for the second layer and w, w W4, w W8, w W8 W4 for
+// the third (W8 = w_8 in the transform's direction, W4 = W8^2: multiplying by
+// it is a swap and a sign).  v = w W8 comes from the pass's root table.
+template <int SIGN>
+__device__ __forceinline__ void bfly_tw(double2 &a, double2 &b, double tx, double ty) {
+  const double y0x = __fma_rn(tx, b.x, __fma_rn(-ty, b.y, a.x));
+  const double y0y = __fma_rn(tx, b.y, __fma_rn(ty, b.x, a.y));
+  b.x = __fma_rn(2.0, a.x, -y0x);
+  b.y = __fma_rn(2.0, a.y, -y0y);
+  a.x = y0x;
+  a.y = y0y;
+}
+// the same with twiddle t W4
+template <int SIGN>
+__device__ __forceinline__ void bfly_tw_rot(double2 &a, double2 &b, double tx, double ty) {
+  if (SIGN < 0) {
+    bfly_tw<SIGN>(a, b, ty, -tx);  // t (-i)
+  } else {
+    bfly_tw<SIGN>(a, b, -ty, tx);  // t i
+  }
+}
+template <int SIGN>
+__device__ __forceinline__ void dft8_tw_fma(double2 *a, double2 w1, double2 w2, double2 w4, double2 v) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q) bfly_tw<SIGN>(a[q], a[q + 4], w4.x, w4.y);
+  bfly_tw<SIGN>(a[0], a[2], w2.x, w2.y);
+  bfly_tw<SIGN>(a[1], a[3], w2.x, w2.y);
+  bfly_tw_rot<SIGN>(a[4], a[6], w2.x, w2.y);
+  bfly_tw_rot<SIGN>(a[5], a[7], w2.x, w2.y);
+  bfly_tw<SIGN>(a[0], a[1], w1.x, w1.y);
+  bfly_tw_rot<SIGN>(a[2], a[3], w1.x, w1.y);
+  bfly_tw<SIGN>(a[4], a[5], v.x, v.y);
+  bfly_tw_rot<SIGN>(a[6], a[7], v.x, v.y);
+  // outputs in bit-reversed places: y0 y4 y2 y6 y1 y5 y3 y7
+  const double2 y1 = a[4], y2 = a[2], y3 = a[6], y4 = a[1], y6 = a[3];
+  a[1] = y1;
+  a[2] = y2;
+  a[3] = y3;
+  a[4] = y4;
+  a[6] = y6;
+}
+
+// The radix-4 stage the same way: A_q = x_q + w^2 x_{q+2} (B: minus), then
+// y0, y2 = A_0 +- w A_1 and y1, y3 = B_0 +- w W4 B_1 (24 FMAs against 28).
+template <int SIGN>
+__device__ __forceinline__ void dft4_tw_fma(double2 *a, double2 w1, double2 w2) {
+  bfly_tw<SIGN>(a[0], a[2], w2.x, w2.y);
+  bfly_tw<SIGN>(a[1], a[3], w2.x, w2.y);
+  bfly_tw<SIGN>(a[0], a[1], w1.x, w1.y);
+  bfly_tw_rot<SIGN>(a[2], a[3], w1.x, w1.y);
+  const double2 y1 = a[2];  // y0 y2 y1 y3 in place
+  a[2] = a[1];
+  a[1] = y1;
+}
+
 // Radix-r butterfly on registers (r <= 8), roots from the pass's table.
 template <typename T, int SIGN>
 __device__ __forceinline__ void butterfly(C2<T> *a, int r, const C2<T> *roots, int nr) {
@@ -738,67 +799,6 @@ __device__ __forceinline__ void pow2_twiddles(const C2<T> *roots, C2<T> *tws, in
   }
 }
 
-// FP64 radix-8 stage with its input twiddles w^q (w = w_{8 LP}^j), as three
-// layers of radix-2 butterflies y0 = a + t b, y1 = 2 a - y0 whose twiddle t
-// is a single complex number: six FMAs per butterfly, 72 per eight values
-// against 80 for seven twiddle products and the 8-point DFT.  With
-// A_q = x_q + w^4 x_{q+4} (B: minus), the even outputs are the 4-point DFT of
-// w^q A_q and the odd ones that of (w W8)^q B_q; the same split again leaves
-// twiddles w^2 and w^2 W4 for the second layer and w, w W4, w W8, w W8 W4 for
-// the third (W8 = w_8 in the transform's direction, W4 = W8^2: multiplying by
-// it is a swap and a sign).  v = w W8 comes from the pass's root table.
-template <int SIGN>
-__device__ __forceinline__ void bfly_tw(double2 &a, double2 &b, double tx, double ty) {
-  const double y0x = __fma_rn(tx, b.x, __fma_rn(-ty, b.y, a.x));
-  const double y0y = __fma_rn(tx, b.y, __fma_rn(ty, b.x, a.y));
-  b.x = __fma_rn(2.0, a.x, -y0x);
-  b.y = __fma_rn(2.0, a.y, -y0y);
-  a.x = y0x;
-  a.y = y0y;
-}
-// the same with twiddle t W4
-template <int SIGN>
-__device__ __forceinline__ void bfly_tw_rot(double2 &a, double2 &b, double tx, double ty) {
-  if (SIGN < 0) {
-    bfly_tw<SIGN>(a, b, ty, -tx);  // t (-i)
-  } else {
-    bfly_tw<SIGN>(a, b, -ty, tx);  // t i
-  }
-}
-template <int SIGN>
-__device__ __forceinline__ void dft8_tw_fma(double2 *a, double2 w1, double2 w2, double2 w4, double2 v) {
-#pragma unroll
-  for (int q = 0; q < 4; ++q) bfly_tw<SIGN>(a[q], a[q + 4], w4.x, w4.y);
-  bfly_tw<SIGN>(a[0], a[2], w2.x, w2.y);
-  bfly_tw<SIGN>(a[1], a[3], w2.x, w2.y);
-  bfly_tw_rot<SIGN>(a[4], a[6], w2.x, w2.y);
-  bfly_tw_rot<SIGN>(a[5], a[7], w2.x, w2.y);
-  bfly_tw<SIGN>(a[0], a[1], w1.x, w1.y);
-  bfly_tw_rot<SIGN>(a[2], a[3], w1.x, w1.y);
-  bfly_tw<SIGN>(a[4], a[5], v.x, v.y);
-  bfly_tw_rot<SIGN>(a[6], a[7], v.x, v.y);
-  // outputs in bit-reversed places: y0 y4 y2 y6 y1 y5 y3 y7
-  const double2 y1 = a[4], y2 = a[2], y3 = a[6], y4 = a[1], y6 = a[3];
-  a[1] = y1;
-  a[2] = y2;
-  a[3] = y3;
-  a[4] = y4;
-  a[6] = y6;
-}
-
-// The radix-4 stage the same way: A_q = x_q + w^2 x_{q+2} (B: minus), then
-// y0, y2 = A_0 +- w A_1 and y1, y3 = B_0 +- w W4 B_1 (24 FMAs against 28).
-template <int SIGN>
-__device__ __forceinline__ void dft4_tw_fma(double2 *a, double2 w1, double2 w2) {
-  bfly_tw<SIGN>(a[0], a[2], w2.x, w2.y);
-  bfly_tw<SIGN>(a[1], a[3], w2.x, w2.y);
-  bfly_tw<SIGN>(a[0], a[1], w1.x, w1.y);
-  bfly_tw_rot<SIGN>(a[2], a[3], w1.x, w1.y);
-  const double2 y1 = a[2];  // y0 y2 y1 y3 in place
-  a[2] = a[1];
-  a[1] = y1;
-}
-
 // The Stockham stage after the first LP points of a power-of-two NF: from
 // the line-padded staging layout (first stage) or the previous stage's
 // swizzled layout, to the next stage's swizzled layout or (last stage) the
@@ -930,10 +930,22 @@ __device__ __forceinline__ void stage_fixed(const C2<T> *in, C2<T> *out, const C
         (void)sexp;
         v = in[pos];
       }
-      if (LP > 1 && q > 0) v = mul<T>(v, root_fx<T, SIGN>(roots, j * q * TSTEP));
+      // (native FP64 radix 8 and 4: the twiddles go into the butterflies below)
+      if (LP > 1 && q > 0 && !(std::is_same<T, double>::value && (R == 8 || R == 4)))
+        v = mul<T>(v, root_fx<T, SIGN>(roots, j * q * TSTEP));
       a[q] = v;
     }
-    bfly_fixed<T, SIGN, R>(a);
+    if constexpr (std::is_same<T, double>::value && (R == 8 || R == 4) && LP > 1) {
+      const C2<T> w1 = root_fx<T, SIGN>(roots, j * TSTEP), w2 = root_fx<T, SIGN>(roots, 2 * j * TSTEP);
+      if constexpr (R == 8) {
+        dft8_tw_fma<SIGN>(a, w1, w2, root_fx<T, SIGN>(roots, 4 * j * TSTEP),
+                          root_fx<T, SIGN>(roots, j * TSTEP + NF / 8));
+      } else {
+        dft4_tw_fma<SIGN>(a, w1, w2);
+      }
+    } else {
+      bfly_fixed<T, SIGN, R>(a);
+    }
 #pragma unroll
     for (int s = 0; s < R; ++s) out[lo + swz<T, NF>((j + s * LP) * M + k)] = a[s];
   }
