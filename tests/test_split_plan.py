@@ -217,3 +217,48 @@ def test_tile_choices_in_the_pass_list():
     assert sp2.radix == api.RADIX_PLAN4
     with pytest.raises(Exception):
         sp2.set_radix(7)
+
+
+def test_native_fp64_tiles_and_paired_split_sides():
+    """Native FP64 passes take tiles of at most 1024 values (two 512-point lines where double-float takes
+    four, whatever tile the plan asks for); the split schedule's sides whose shared dimension is a sum of
+    sub-axis parts walk as separable ("(paired)"), while a start decomposition with uneven blocks (per-rank
+    strides) keeps the per-value walk."""
+    import re
+    comm = api.Comm(64)
+    blk, rotd, frv = _bench_specs(512)
+    D = api.decomp_from_spec(comm, frv)
+    probe = api.SplitPlan(D, 1 << 20, 1 << 40, 1 << 21)
+    length = 2 * probe.extent64
+    sp = api.SplitPlan(D, 1 << 20, length, 1 << 21)
+
+    def lines():
+        return [int(x) for x in re.findall(r" x(\d+) v2", sp.describe())]
+
+    assert lines() == [4, 4, 4]
+    sp.set_arith(api.ARITH_FP64)
+    assert lines() == [2, 2, 2]
+    sp.set_tile(4096)
+    assert lines() == [2, 2, 2]
+    sp.set_tile(512)
+    assert lines() == [1, 1, 1]
+    sp.set_tile(0)
+    sp.set_schedule(api.SCHEDULE_SPLIT)
+    d = sp.describe()
+    assert d.count("(paired)") == 12 and "shared dim" not in d, d
+    # 4 x 3 ranks: 30 values in blocks of 8 (uneven), so the first pass reads the start layout per value
+    comm2 = api.Comm(12)
+    D2 = api.decomp_from_spec(comm2, "packed:block(30,4)|block(28,3)|local(12)")
+    sp2 = api.SplitPlan(D2, 1 << 20, 1 << 20, 1 << 21, B=[3, 4, 2])
+    sp2.set_schedule(api.SCHEDULE_SPLIT)
+    d2 = sp2.describe()
+    first = re.findall(r"\[t=\d[^\]]*\]", d2)[0]
+    assert "in=atb(per value)" in first and "(paired)" in d2, d2
+
+
+def _bench_specs(n):
+    g0 = g1 = 8
+    blk = "packed:block(%d,%d)|block(%d,%d)|local(%d)" % (n, g0, n, g1, n)
+    rotd = "packed:rotate(1,block(%d,%d))|rotate(%d,block(%d,%d))|local(%d)" % (n, g0, n // 3, n, g1, n)
+    frv = "packed:frev(16,%d,block(%d,%d))|frev(%d,16,block(%d,%d))|local(%d)" % (n // 16, n, g0, n // 16, n, g1, n)
+    return blk, rotd, frv
