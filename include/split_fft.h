@@ -217,11 +217,12 @@ int dmg_split_set_schedule(SplitPlan plan, int schedule);
 /** The schedule in use: DMG_SCHEDULE_LINES or DMG_SCHEDULE_SPLIT. */
 int dmg_split_get_schedule(SplitPlan plan);
 /** Values per pass tile: 0 for the default (4096 for complex64, 2048 for
- * complex128), else a power of two from 64 up to twice that.  Smaller tiles
- * hold fewer lines side by side; larger ones run the FP32 and double-float
- * passes of power-of-two lengths 256...2048 in one 512-thread block per SM (other
- * passes keep the default), so that passes whose lines are strided in memory
- * move longer rows. */
+ * complex128 in double-float, 1024 in native FP64), else a power of two from
+ * 64 up to twice that.  Smaller tiles hold fewer lines side by side; larger
+ * ones run the FP32 and double-float passes of power-of-two lengths
+ * 256...2048 in one 512-thread block per SM (other passes keep the default),
+ * so that passes whose lines are strided in memory move longer rows.  Native
+ * FP64 passes take at most 1024 values (one line where a line is longer). */
 int dmg_split_set_tile(SplitPlan plan, int values);
 /** The plan's values per tile as set (0: the default, which gives FP32
  * passes whose lines are strided in memory the wide tiles and the others
